@@ -1,0 +1,312 @@
+"""Benchmark: DF Fock builds (J + K) per second on one GB300.
+
+Workload (default): n-C20H42, cc-pVDZ / cc-pVDZ-jkfit, atom blocks, Schwarz
+1e-10 (nbf 490, naux 2366, nocc 81), 3-center tensor resident in HBM; one
+step = one Fock build (DF-J + DF-MO-K) at the core-guess density.  The
+tensor (3 GB) is larger than L2, so no extra flush runs between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--precision fp64|split]
+  python bench.py --impl reference ...   # CPU restatement on the host cores
+
+N > 1 (torchrun): replicas only; every rank builds on its own GPU, the time
+is the max over ranks and the value the sum of builds/s.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Fock builds/s (DF-J + DF-K)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--alkane", type=int, default=20)
+    ap.add_argument("--kmethod", default="dfmo")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def setup(nC):
+    from chem_gb300 import geometry
+    from chem_gb300.dfsystem import build_dfsystem
+    from chem_gb300.molecule import molecule_from_angstrom
+    s, x = geometry.alkane(nC)
+    mol = molecule_from_angstrom(s, x, "cc-pvdz", "cc-pvdz-jkfit")
+    t0 = time.perf_counter()
+    ds = build_dfsystem(mol, eps=1e-10)
+    tset = time.perf_counter() - t0
+    # core-guess orbitals: diagonalise H in the Loewdin basis
+    sv, U = np.linalg.eigh(ds.S)
+    X = U @ np.diag(sv ** -0.5) @ U.T
+    e, Cp = np.linalg.eigh(X.T @ ds.Hcore @ X)
+    Cocc = np.ascontiguousarray((X @ Cp)[:, :mol.nocc])
+    P = Cocc @ Cocc.T
+    return mol, ds, Cocc, P, tset
+
+
+def workload_config(ds, mol, nC, precision, world):
+    return {
+        "workload": f"C{nC}H{2 * nC + 2} DF-HF Fock build, cc-pVDZ/cc-pVDZ-jkfit, atom blocks, "
+                    f"Schwarz 1e-10",
+        "nbf": ds.nbf, "naux": ds.naux, "nocc": mol.nocc, "nnz_B": ds.layout.nnz,
+        "kept_block_pairs": round(ds.layout.kept_block_fraction(), 4),
+        "precision": precision, "kmethod": "dfmo", "jmethod": "dfao",
+        "l2_flush": "none: resident 3-center tensor (%.2f GB) exceeds L2" % (ds.layout.nnz * 8e-9),
+        "parallelism": f"replicas x{world}",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.idx = device_index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+
+    def _run(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.idx),
+                                      "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([v.strip() for v in out.split(",")])
+            except Exception:
+                pass
+            self._stop.wait(0.2)
+
+    def __enter__(self):
+        self._t = threading.Thread(target=self._run, daemon=True)
+        self._t.start()
+        return self
+
+    def __exit__(self, *a):
+        self._stop.set()
+        self._t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        mx = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for s in self.samples:
+            for n, v in zip(names, s[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(self.samples)}
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d["hbm_gbs"], d["bf16_tflops"], d.get("bf16_tflops_sustained"), "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def cpu_reference_build(ds, Cocc, P, kchunk):
+    """One Fock build with the CPU oracle on all host threads (seconds)."""
+    from oracle.oracle import Oracle
+    O = Oracle(ds.layout, ds.B)
+    t0 = time.perf_counter()
+    O.df_j(ds.Vinv, 2.0 * P, ds.eps)
+    O.dfmo_k(np.tril(ds.Linv), Cocc, ds.eps, kchunk=kchunk)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mol, ds, Cocc, P, _ = setup(args.alkane)
+    ncores = os.cpu_count()
+    times = []
+    for i in range(args.warmup + args.steps):
+        t = cpu_reference_build(ds, Cocc, P, 0)
+        if i >= args.warmup:
+            times.append(t)
+    tot = sum(times)
+    val = len(times) / tot
+    cfg = workload_config(ds, mol, args.alkane, "fp64", 1)
+    print(json.dumps({
+        "metric": METRIC, "value": val, "unit": "builds/s", "impl": "reference",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * tot / len(times), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic molecule (seed-free alkane rule)",
+        "config": cfg,
+        "cpu_baseline": {"value": val, "unit": "builds/s", "cores": ncores, "kind": "port",
+                         "sample": "full Fock build (DF-J + DF-MO-K) per step, C restatement, "
+                                   f"OpenMP on {ncores} threads"},
+        "e2e": {"value": val, "unit": "builds/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+
+    from chem_gb300.fock import JKEngine, k_split_plan
+
+    mol, ds, Cocc, P, tset = setup(args.alkane)
+    eng = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=ds.eps, device=local,
+                   precision=args.precision)
+    dev = torch.device("cuda", local)
+    dP = torch.from_numpy(2.0 * P).to(dev)
+    dC = torch.from_numpy(Cocc).to(dev)
+    n = ds.nbf
+    dJ = torch.empty((n, n), dtype=torch.float64, device=dev)
+    dK = torch.empty((n, n), dtype=torch.float64, device=dev)
+    torch.cuda.synchronize()
+    stream = torch.cuda.ExternalStream(eng.stream, device=dev)
+
+    def step():
+        eng.compute_jk_dev(dP.data_ptr(), dC.data_ptr(), mol.nocc, dJ.data_ptr(), dK.data_ptr(),
+                           args.kmethod)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    eng.synchronize()
+
+    # timed region: device-resident inputs, CUDA events on the engine stream
+    launches0 = eng.kernel_launches
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        eng.synchronize()
+    torch.cuda.synchronize()
+    launches = eng.kernel_launches - launches0
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1e3 / ms
+
+    # per-phase device time (CUDA events around every launch), same steps
+    eng.profile(True)
+    for _ in range(args.steps):
+        step()
+    eng.synchronize()
+    prof = eng.profile_read()
+    eng.profile(False)
+
+    # end to end through the public host API: H2D of P and C, D2H of J and K
+    Ph = np.ascontiguousarray(2.0 * P)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    eng.compute_jk(Ph, Cocc, args.kmethod)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        Jh, Kh = eng.compute_jk(Ph, Cocc, args.kmethod)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    # roofline of the dominant phase
+    hbm, bf16, bf16s, src = peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][0])
+    name, (tms, nl) = top
+    per_launch_ms = tms / max(1, nl)
+    nbf, naux, nocc, nnz = ds.nbf, ds.naux, mol.nocc, ds.layout.nnz
+    flops = {
+        "half_transform": 2.0 * nocc * nnz,
+        "fit": 2.0 * naux * naux * nbf * nocc / 2.0,  # lower-triangular L^-1
+        "k_gemm": 1.0 * naux * nocc * nbf * (nbf + 1),
+    }
+    roof = None
+    if name in flops:
+        fp64_peak = 1250.0  # GB300 nominal FP64 (GFLOP/s), not in MEASURED_PEAKS.json
+        ach = flops[name] / (per_launch_ms * 1e-3) / 1e12
+        roof = {"kernel": name, "bound": "fp64", "achieved": ach, "peak": fp64_peak / 1e3,
+                "unit": "TFLOP/s", "frac": ach / (fp64_peak / 1e3), "traffic": None,
+                "peak_source": "nominal FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)",
+                "algorithmic_flops_per_launch": flops[name], "ms_per_launch": per_launch_ms}
+    elif name in ("j_rowdot", "j_colsum"):
+        byts = nnz * 8.0
+        ach = byts / (per_launch_ms * 1e-3) / 1e9
+        roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
+                "frac": ach / hbm, "traffic": None, "peak_source": src,
+                "algorithmic_bytes_per_launch": byts, "ms_per_launch": per_launch_ms}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic molecule (seed-free alkane rule), host-computed integrals",
+        "config": workload_config(ds, mol, args.alkane, args.precision, world),
+        "e2e": {"value": world * 1e3 / e2e_ms, "unit": "builds/s",
+                "h2d_bytes_per_step": int(Ph.nbytes + Cocc.nbytes),
+                "d2h_bytes_per_step": int(2 * n * n * 8)},
+        "gpu_launches": int(launches),
+        "roofline": roof,
+        "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[1]},
+        "clocks": clk.summary(),
+        "setup_s": {"integrals_host": round(tset, 2)},
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        kc = k_split_plan(nbf, naux, nocc)[1]
+        tcpu = cpu_reference_build(ds, Cocc, P, kc)
+        out["cpu_baseline"] = {"value": 1.0 / tcpu, "unit": "builds/s", "cores": os.cpu_count(),
+                               "kind": "port",
+                               "sample": "one full Fock build (DF-J + DF-MO-K), C restatement, "
+                                         f"OpenMP on {os.cpu_count()} threads"}
+    eng.close()
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,721 @@
+// libgbjk: context, device memory and the C-ABI of the DF J/K engine.
+//
+// The context owns the resident 3-center tensor (panel layout), the metric
+// factors, per-nocc workspaces and the launch plans (tile lists) of every
+// contraction.  One compute call issues a fixed sequence of launches on the
+// context's stream:
+//   J:  gather P rows -> row dots (g partials) -> reduce -> h = V^-1 g
+//       -> column sums J = B^T h -> block filter
+//   K:  gather C rows -> half transform H = B C (grouped GEMM over panels)
+//       -> fit (L^-1 or V^-1, batched over mu) -> K = -Hfit^T Hfit (split-K)
+//       -> reduce -> block filter
+// The split-precision path (kernels_split.cuh) replaces the three GEMMs.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "common.cuh"
+#include "gbjk.h"
+#include "kernels_fp64.cuh"
+#include "split_gemm.cuh"
+
+using namespace gbjk;
+
+enum Phase {
+  PH_GATHER = 0,
+  PH_J_ROWDOT,
+  PH_J_REDUCE,
+  PH_J_METRIC,
+  PH_J_COLSUM,
+  PH_HT,
+  PH_FIT,
+  PH_KGEMM,
+  PH_KREDUCE,
+  PH_FILTER,
+  PH_SPLIT,
+  PH_COUNT
+};
+static const char* kPhaseNames[PH_COUNT] = {
+    "gather", "j_rowdot", "j_reduce", "j_metric", "j_colsum", "half_transform",
+    "fit",    "k_gemm",   "k_reduce", "filter",   "split_operands"};
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct gbjk_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int64_t launches = 0;
+  size_t dev_bytes = 0;
+  std::unordered_map<void*, size_t> alloc_bytes;
+  // layout (host)
+  int nbf = 0, naux = 0, nblk = 0;
+  double eps = 0.0;
+  std::vector<int> bsize, boff, panelK, cmoff, colmap, blk_of;
+  std::vector<long long> panel_off, pg_off;
+  long long nnz = 0, pg_total = 0;
+  int ncols_total = 0, maxK = 0;
+  // layout (device)
+  int *d_blk_of = nullptr, *d_boff = nullptr, *d_panelK = nullptr, *d_cmoff = nullptr,
+      *d_colmap = nullptr;
+  long long *d_panel_off = nullptr, *d_pg_off = nullptr;
+  // resident data
+  double* d_B = nullptr;
+  double *d_Linv = nullptr, *d_Vinv = nullptr;
+  bool have_B = false, have_metric = false;
+  bool colsum_smem_set = false;
+  // J workspace
+  double *d_P = nullptr, *d_Pg = nullptr, *d_part = nullptr, *d_g = nullptr, *d_h = nullptr,
+         *d_J = nullptr;
+  // K workspace (per nocc)
+  int ws_nocc = -1;
+  int ksplit = 1;
+  double *d_C = nullptr, *d_Cg = nullptr, *d_H = nullptr, *d_H2 = nullptr, *d_Kpart = nullptr,
+         *d_K = nullptr;
+  GemmGroup* d_groups = nullptr;
+  GemmTile* d_tiles = nullptr;
+  int n_ht_groups = 0, n_fit_groups = 0;
+  int ht_tile0 = 0, ht_ntiles = 0, fit_tile0 = 0, fit_ntiles = 0, fitV_tile0 = 0, syrk_tile0 = 0,
+      syrk_ntiles = 0, lmo_tile0 = 0, lmo_ntiles = 0;
+  int fitL_group0 = 0, fitV_group0 = 0, syrk_group = 0, lmo_group = 0;
+  // precision
+  int precision = GBJK_FP64;
+  int nslices = 0;
+  SplitState split;
+  // profiling
+  bool profile = false;
+  cudaEvent_t ev[PH_COUNT][2] = {};
+  double ph_ms[PH_COUNT] = {};
+  int64_t ph_launch[PH_COUNT] = {};
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+  std::vector<cudaEvent_t> ev_pool;
+};
+
+namespace {
+
+gbjk_status fail(gbjk_ctx* c, gbjk_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+#define CK(call)                                                                         \
+  do {                                                                                   \
+    cudaError_t e_ = (call);                                                             \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, e_ == cudaErrorMemoryAllocation ? GBJK_OOM : GBJK_CUDA_ERROR,     \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));                   \
+  } while (0)
+
+#define CKL(phase)                                                                       \
+  do {                                                                                   \
+    ctx->launches++;                                                                     \
+    cudaError_t e_ = cudaGetLastError();                                                 \
+    if (e_ != cudaSuccess)                                                               \
+      return fail(ctx, GBJK_CUDA_ERROR,                                                  \
+                  std::string("launch ") + kPhaseNames[phase] + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+gbjk_status dalloc(gbjk_ctx* ctx, T** p, size_t count) {
+  if (*p) return GBJK_OK;
+  if (count == 0) count = 1;
+  cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(ctx, GBJK_OOM,
+                "cudaMalloc of " + std::to_string(count * sizeof(T)) + " bytes failed: " +
+                    cudaGetErrorString(e));
+  }
+  ctx->alloc_bytes[(void*)*p] = count * sizeof(T);
+  ctx->dev_bytes += count * sizeof(T);
+  return GBJK_OK;
+}
+
+template <class T>
+void dfree(gbjk_ctx* ctx, T** p) {
+  if (*p) {
+    cudaFree(*p);
+    auto it = ctx->alloc_bytes.find((void*)*p);
+    if (it != ctx->alloc_bytes.end()) {
+      ctx->dev_bytes -= it->second;
+      ctx->alloc_bytes.erase(it);
+    }
+    *p = nullptr;
+  }
+}
+
+cudaEvent_t get_event(gbjk_ctx* ctx) {
+  if (!ctx->ev_pool.empty()) {
+    cudaEvent_t e = ctx->ev_pool.back();
+    ctx->ev_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+
+struct PhaseScope {
+  gbjk_ctx* ctx;
+  int ph;
+  cudaEvent_t a = nullptr, b = nullptr;
+  PhaseScope(gbjk_ctx* c, int p) : ctx(c), ph(p) {
+    if (ctx->profile) {
+      a = get_event(ctx);
+      b = get_event(ctx);
+      cudaEventRecord(a, ctx->stream);
+    }
+  }
+  ~PhaseScope() {
+    if (ctx->profile) {
+      cudaEventRecord(b, ctx->stream);
+      ctx->pending.push_back({ph, {a, b}});
+    }
+    ctx->ph_launch[ph]++;
+  }
+};
+
+void resolve_profile(gbjk_ctx* ctx) {
+  for (auto& pe : ctx->pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, pe.second.first, pe.second.second) == cudaSuccess)
+      ctx->ph_ms[pe.first] += ms;
+    ctx->ev_pool.push_back(pe.second.first);
+    ctx->ev_pool.push_back(pe.second.second);
+  }
+  ctx->pending.clear();
+}
+
+int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+void add_tiles(std::vector<GemmTile>& tiles, int group, int M, int N, int k0, int k1,
+               long long coff, bool upper_only) {
+  for (int mt = 0; mt < cdiv(M, 64); ++mt)
+    for (int nt = 0; nt < cdiv(N, 64); ++nt) {
+      if (upper_only && nt < mt) continue;
+      tiles.push_back({group, mt, nt, k0, k1, coff});
+    }
+}
+
+// (Re)build the K workspaces and launch plans for a given nocc.
+gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
+  if (ctx->ws_nocc == nocc) return GBJK_OK;
+  const size_t nbf = ctx->nbf, naux = ctx->naux;
+  const size_t hsz = nbf * naux * nocc;
+  dfree(ctx, &ctx->d_C);
+  dfree(ctx, &ctx->d_Cg);
+  dfree(ctx, &ctx->d_H);
+  dfree(ctx, &ctx->d_H2);
+  dfree(ctx, &ctx->d_Kpart);
+  dfree(ctx, &ctx->d_groups);
+  dfree(ctx, &ctx->d_tiles);
+  ctx->ws_nocc = -1;
+  gbjk_status s;
+  if ((s = dalloc(ctx, &ctx->d_C, nbf * nocc))) return s;
+  if ((s = dalloc(ctx, &ctx->d_Cg, (size_t)ctx->ncols_total * nocc))) return s;
+  if ((s = dalloc(ctx, &ctx->d_H, hsz))) return s;
+  if ((s = dalloc(ctx, &ctx->d_H2, hsz))) return s;
+  // split-K of the exchange GEMM: enough tiles to fill the GPU
+  const long long kdim = (long long)naux * nocc;
+  int ks = 1;
+  long long kchunk64 = kdim;
+  gbjk_k_split_plan(ctx->nbf, ctx->naux, nocc, &ks, &kchunk64);
+  ctx->ksplit = ks;
+  if ((s = dalloc(ctx, &ctx->d_Kpart, (size_t)ks * nbf * nbf))) return s;
+
+  std::vector<GemmGroup> groups;
+  std::vector<GemmTile> tiles;
+  // half transform: one group per panel
+  ctx->ht_tile0 = 0;
+  for (int I = 0; I < ctx->nblk; ++I) {
+    GemmGroup g;
+    g.A = ctx->d_B + ctx->panel_off[I];
+    g.B = ctx->d_Cg + (long long)ctx->cmoff[I] * nocc;
+    g.C = ctx->d_H + (long long)ctx->boff[I] * naux * nocc;
+    g.M = ctx->bsize[I] * (int)naux;
+    g.N = nocc;
+    g.K = ctx->panelK[I];
+    g.lda = ctx->panelK[I];
+    g.ldb = nocc;
+    g.ldc = nocc;
+    g.flags = 0;
+    if (g.K == 0) continue;
+    add_tiles(tiles, (int)groups.size(), g.M, g.N, 0, g.K, 0, false);
+    groups.push_back(g);
+  }
+  ctx->ht_ntiles = (int)tiles.size();
+  // fit with L^-1 (lower) : per mu, H2[mu] = Linv H[mu]
+  ctx->fit_tile0 = (int)tiles.size();
+  ctx->fitL_group0 = (int)groups.size();
+  for (size_t mu = 0; mu < nbf; ++mu) {
+    GemmGroup g;
+    g.A = ctx->d_Linv;
+    g.B = ctx->d_H + mu * naux * nocc;
+    g.C = ctx->d_H2 + mu * naux * nocc;
+    g.M = (int)naux;
+    g.N = nocc;
+    g.K = (int)naux;
+    g.lda = (int)naux;
+    g.ldb = nocc;
+    g.ldc = nocc;
+    g.flags = kLowerA;
+    add_tiles(tiles, (int)groups.size(), g.M, g.N, 0, g.K, 0, false);
+    groups.push_back(g);
+  }
+  ctx->fit_ntiles = (int)tiles.size() - ctx->fit_tile0;
+  // fit with V^-1 (full) for DF-LMO: same shapes, groups pointing at V^-1
+  ctx->fitV_group0 = (int)groups.size();
+  for (size_t mu = 0; mu < nbf; ++mu) {
+    GemmGroup g = groups[ctx->fitL_group0 + mu];
+    g.A = ctx->d_Vinv;
+    g.flags = 0;
+    groups.push_back(g);
+  }
+  ctx->fitV_tile0 = (int)tiles.size();
+  for (int t = 0; t < ctx->fit_ntiles; ++t) {
+    GemmTile tt = tiles[ctx->fit_tile0 + t];
+    tt.group += ctx->fitV_group0 - ctx->fitL_group0;
+    tiles.push_back(tt);
+  }
+  // exchange GEMM (DF-MO): K = -H2^T H2, upper tiles, split-K
+  const int kchunk = (int)kchunk64;
+  {
+    GemmGroup g;
+    g.A = ctx->d_H2;
+    g.B = ctx->d_H2;
+    g.C = ctx->d_Kpart;
+    g.M = (int)nbf;
+    g.N = (int)nbf;
+    g.K = (int)kdim;
+    g.lda = (int)kdim;
+    g.ldb = (int)kdim;
+    g.ldc = (int)nbf;
+    g.flags = kTransB;
+    ctx->syrk_group = (int)groups.size();
+    groups.push_back(g);
+    ctx->syrk_tile0 = (int)tiles.size();
+    for (int k = 0; k < ks; ++k) {
+      const int k0 = k * kchunk, k1 = (int)std::min<long long>(kdim, (long long)(k + 1) * kchunk);
+      add_tiles(tiles, ctx->syrk_group, g.M, g.N, k0, std::max(k0, k1), (long long)k * nbf * nbf,
+                true);
+    }
+    ctx->syrk_ntiles = (int)tiles.size() - ctx->syrk_tile0;
+  }
+  // exchange GEMM (DF-LMO): K_nm = -sum H[m] Hfit[n]  -> rows n from H2 (Hfit), cols m from H
+  {
+    GemmGroup g;
+    g.A = ctx->d_H2;
+    g.B = ctx->d_H;
+    g.C = ctx->d_Kpart;
+    g.M = (int)nbf;
+    g.N = (int)nbf;
+    g.K = (int)kdim;
+    g.lda = (int)kdim;
+    g.ldb = (int)kdim;
+    g.ldc = (int)nbf;
+    g.flags = kTransB;
+    ctx->lmo_group = (int)groups.size();
+    groups.push_back(g);
+    ctx->lmo_tile0 = (int)tiles.size();
+    for (int k = 0; k < ks; ++k) {
+      const int k0 = k * kchunk, k1 = (int)std::min<long long>(kdim, (long long)(k + 1) * kchunk);
+      add_tiles(tiles, ctx->lmo_group, g.M, g.N, k0, std::max(k0, k1), (long long)k * nbf * nbf,
+                false);
+    }
+    ctx->lmo_ntiles = (int)tiles.size() - ctx->lmo_tile0;
+  }
+  if ((s = dalloc(ctx, &ctx->d_groups, groups.size()))) return s;
+  if ((s = dalloc(ctx, &ctx->d_tiles, tiles.size()))) return s;
+  CK(cudaMemcpy(ctx->d_groups, groups.data(), groups.size() * sizeof(GemmGroup),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_tiles, tiles.data(), tiles.size() * sizeof(GemmTile),
+                cudaMemcpyHostToDevice));
+  ctx->ws_nocc = nocc;
+  return GBJK_OK;
+}
+
+gbjk_status ensure_j_workspace(gbjk_ctx* ctx) {
+  gbjk_status s;
+  const size_t nbf = ctx->nbf, naux = ctx->naux;
+  if ((s = dalloc(ctx, &ctx->d_P, nbf * nbf))) return s;
+  if ((s = dalloc(ctx, &ctx->d_Pg, (size_t)ctx->pg_total))) return s;
+  if ((s = dalloc(ctx, &ctx->d_part, nbf * naux))) return s;
+  if ((s = dalloc(ctx, &ctx->d_g, naux))) return s;
+  if ((s = dalloc(ctx, &ctx->d_h, naux))) return s;
+  if ((s = dalloc(ctx, &ctx->d_J, nbf * nbf))) return s;
+  if ((s = dalloc(ctx, &ctx->d_K, nbf * nbf))) return s;
+  return GBJK_OK;
+}
+
+gbjk_status launch_gemm(gbjk_ctx* ctx, int tile0, int ntiles, bool transB, double alpha,
+                        int phase) {
+  if (ntiles == 0) return GBJK_OK;
+  PhaseScope ps(ctx, phase);
+  if (transB)
+    k_gemm_fp64<true><<<ntiles, 256, 0, ctx->stream>>>(ctx->d_groups, ctx->d_tiles + tile0, alpha);
+  else
+    k_gemm_fp64<false><<<ntiles, 256, 0, ctx->stream>>>(ctx->d_groups, ctx->d_tiles + tile0, alpha);
+  CKL(phase);
+  return GBJK_OK;
+}
+
+gbjk_status filter(gbjk_ctx* ctx, double* M) {
+  if (ctx->eps <= 0) return GBJK_OK;
+  PhaseScope ps(ctx, PH_FILTER);
+  k_block_filter<<<dim3(ctx->nblk, ctx->nblk), 128, 0, ctx->stream>>>(M, ctx->nbf, ctx->d_boff,
+                                                                      ctx->eps);
+  CKL(PH_FILTER);
+  return GBJK_OK;
+}
+
+gbjk_status run_j(gbjk_ctx* ctx, const double* dP, double* dJ) {
+  const int nbf = ctx->nbf, naux = ctx->naux;
+  {
+    PhaseScope ps(ctx, PH_GATHER);
+    k_gather_panel_rows<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, 0, ctx->stream>>>(
+        dP, nbf, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK, ctx->d_pg_off, ctx->d_cmoff,
+        ctx->d_colmap, ctx->d_Pg);
+    CKL(PH_GATHER);
+  }
+  {
+    PhaseScope ps(ctx, PH_J_ROWDOT);
+    const long long rows = (long long)nbf * naux;
+    k_j_rowdot<<<cdiv(rows * 32, 256), 256, 0, ctx->stream>>>(
+        ctx->d_B, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK, ctx->d_pg_off,
+        ctx->d_Pg, nbf, naux, ctx->d_part);
+    CKL(PH_J_ROWDOT);
+  }
+  {
+    PhaseScope ps(ctx, PH_J_REDUCE);
+    k_reduce_rows<<<cdiv(naux, 128), 128, 0, ctx->stream>>>(ctx->d_part, nbf, naux, ctx->d_g);
+    CKL(PH_J_REDUCE);
+  }
+  {
+    PhaseScope ps(ctx, PH_J_METRIC);
+    k_gemv<<<cdiv((long long)naux * 32, 256), 256, 0, ctx->stream>>>(ctx->d_Vinv, ctx->d_g, naux,
+                                                                       ctx->d_h);
+    CKL(PH_J_METRIC);
+  }
+  {
+    PhaseScope ps(ctx, PH_J_COLSUM);
+    const size_t hbytes = (size_t)naux * sizeof(double);
+    if (hbytes > 48 * 1024 && !ctx->colsum_smem_set) {
+      CK(cudaFuncSetAttribute(k_j_colsum, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)hbytes));
+      ctx->colsum_smem_set = true;
+    }
+    k_j_colsum<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, naux * sizeof(double), ctx->stream>>>(
+        ctx->d_B, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK, ctx->d_cmoff,
+        ctx->d_colmap, ctx->d_h, nbf, naux, dJ);
+    CKL(PH_J_COLSUM);
+  }
+  return filter(ctx, dJ);
+}
+
+gbjk_status run_k(gbjk_ctx* ctx, int kmethod, const double* dC, int nocc, double* dK) {
+  gbjk_status s;
+  if ((s = ensure_k_workspace(ctx, nocc))) return s;
+  const int nbf = ctx->nbf;
+  {
+    PhaseScope ps(ctx, PH_GATHER);
+    const long long total = (long long)ctx->ncols_total * nocc;
+    k_gather_cols<<<cdiv(total, 256), 256, 0, ctx->stream>>>(dC, nocc, ctx->d_colmap,
+                                                             ctx->ncols_total, ctx->d_Cg);
+    CKL(PH_GATHER);
+  }
+  if (ctx->precision == GBJK_SPLIT_BF16) {
+    if ((s = split_run_k(ctx->split, ctx->stream, kmethod, nocc, dK, &ctx->launches, &ctx->err)))
+      return s;
+    return filter(ctx, dK);
+  }
+  if ((s = launch_gemm(ctx, ctx->ht_tile0, ctx->ht_ntiles, false, 1.0, PH_HT))) return s;
+  const bool mo = kmethod == GBJK_K_DFMO;
+  if ((s = launch_gemm(ctx, mo ? ctx->fit_tile0 : ctx->fitV_tile0, ctx->fit_ntiles, false, 1.0,
+                       PH_FIT)))
+    return s;
+  if ((s = launch_gemm(ctx, mo ? ctx->syrk_tile0 : ctx->lmo_tile0,
+                       mo ? ctx->syrk_ntiles : ctx->lmo_ntiles, true, 1.0, PH_KGEMM)))
+    return s;
+  {
+    PhaseScope ps(ctx, PH_KREDUCE);
+    const long long n2 = (long long)nbf * nbf;
+    k_splitk_reduce<<<cdiv(n2, 256), 256, 0, ctx->stream>>>(ctx->d_Kpart, ctx->ksplit, nbf, -1.0,
+                                                            mo ? 1 : 0, dK);
+    CKL(PH_KREDUCE);
+  }
+  return filter(ctx, dK);
+}
+
+}  // namespace
+
+extern "C" {
+
+gbjk_status gbjk_k_split_plan(int nbf, int naux, int nocc, int* ksplit, long long* kchunk) {
+  if (nbf <= 0 || naux <= 0 || nocc <= 0 || !ksplit || !kchunk) return GBJK_INVALID_ARG;
+  const long long kdim = (long long)naux * nocc;
+  const int nt = (nbf + 63) / 64;
+  const int ntile_upper = nt * (nt + 1) / 2;
+  int ks = std::max(1, std::min<int>(64, 4 * 152 / std::max(1, ntile_upper)));
+  while (ks > 1 && kdim / ks < 256) --ks;
+  long long kc = ((kdim + ks - 1) / ks + 15) / 16 * 16;
+  ks = (int)((kdim + kc - 1) / kc);
+  *ksplit = ks;
+  *kchunk = kc;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_create(gbjk_ctx** out, const gbjk_desc* d) {
+  if (!out || !d) return GBJK_INVALID_ARG;
+  *out = nullptr;
+  if (d->nbf <= 0 || d->naux <= 0 || d->nblk <= 0 || !d->blk_size || !d->panel_K || !d->colmap)
+    return GBJK_INVALID_ARG;
+  if ((size_t)d->naux * sizeof(double) > 200 * 1024) return GBJK_INVALID_ARG;
+  auto* ctx = new (std::nothrow) gbjk_ctx;
+  if (!ctx) return GBJK_OOM;
+  ctx->device = d->device;
+  ctx->nbf = d->nbf;
+  ctx->naux = d->naux;
+  ctx->nblk = d->nblk;
+  ctx->eps = d->filter_eps;
+  ctx->bsize.assign(d->blk_size, d->blk_size + d->nblk);
+  ctx->panelK.assign(d->panel_K, d->panel_K + d->nblk);
+  ctx->boff.assign(d->nblk + 1, 0);
+  ctx->cmoff.assign(d->nblk + 1, 0);
+  ctx->panel_off.assign(d->nblk, 0);
+  ctx->pg_off.assign(d->nblk, 0);
+  long long po = 0, pg = 0;
+  for (int I = 0; I < d->nblk; ++I) {
+    if (d->blk_size[I] <= 0 || d->panel_K[I] < 0 || d->panel_K[I] > d->nbf) {
+      delete ctx;
+      return GBJK_INVALID_ARG;
+    }
+    ctx->boff[I + 1] = ctx->boff[I] + d->blk_size[I];
+    ctx->cmoff[I + 1] = ctx->cmoff[I] + d->panel_K[I];
+    ctx->panel_off[I] = po;
+    ctx->pg_off[I] = pg;
+    po += (long long)d->blk_size[I] * d->naux * d->panel_K[I];
+    pg += (long long)d->blk_size[I] * d->panel_K[I];
+    ctx->maxK = std::max(ctx->maxK, d->panel_K[I]);
+  }
+  if (ctx->boff[d->nblk] != d->nbf) {
+    delete ctx;
+    return GBJK_INVALID_ARG;
+  }
+  ctx->nnz = po;
+  ctx->pg_total = pg;
+  ctx->ncols_total = ctx->cmoff[d->nblk];
+  ctx->colmap.assign(d->colmap, d->colmap + ctx->ncols_total);
+  for (int c : ctx->colmap)
+    if (c < 0 || c >= d->nbf) {
+      delete ctx;
+      return GBJK_INVALID_ARG;
+    }
+  ctx->blk_of.resize(d->nbf);
+  for (int I = 0; I < d->nblk; ++I)
+    for (int m = ctx->boff[I]; m < ctx->boff[I + 1]; ++m) ctx->blk_of[m] = I;
+
+  if (cudaSetDevice(ctx->device) != cudaSuccess) {
+    delete ctx;
+    return GBJK_CUDA_ERROR;
+  }
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete ctx;
+    return GBJK_CUDA_ERROR;
+  }
+  gbjk_status s;
+  auto up = [&](auto** dptr, const auto& vec) -> gbjk_status {
+    gbjk_status st = dalloc(ctx, dptr, vec.size());
+    if (st) return st;
+    if (cudaMemcpy(*dptr, vec.data(), vec.size() * sizeof(vec[0]), cudaMemcpyHostToDevice) !=
+        cudaSuccess)
+      return fail(ctx, GBJK_CUDA_ERROR, "layout upload failed");
+    return GBJK_OK;
+  };
+  if ((s = up(&ctx->d_blk_of, ctx->blk_of)) || (s = up(&ctx->d_boff, ctx->boff)) ||
+      (s = up(&ctx->d_panelK, ctx->panelK)) || (s = up(&ctx->d_cmoff, ctx->cmoff)) ||
+      (s = up(&ctx->d_colmap, ctx->colmap)) || (s = up(&ctx->d_panel_off, ctx->panel_off)) ||
+      (s = up(&ctx->d_pg_off, ctx->pg_off))) {
+    gbjk_destroy(ctx);
+    return s;
+  }
+  ctx->split.init(ctx->nbf, ctx->naux, ctx->nblk, ctx->bsize, ctx->boff, ctx->panelK, ctx->cmoff,
+                  ctx->panel_off);
+  *out = ctx;
+  return GBJK_OK;
+}
+
+void gbjk_destroy(gbjk_ctx* ctx) {
+  if (!ctx) return;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->split.release();
+  void* ptrs[] = {ctx->d_blk_of, ctx->d_boff,  ctx->d_panelK, ctx->d_cmoff, ctx->d_colmap,
+                  ctx->d_panel_off, ctx->d_pg_off, ctx->d_B, ctx->d_Linv, ctx->d_Vinv,
+                  ctx->d_P, ctx->d_Pg, ctx->d_part, ctx->d_g, ctx->d_h, ctx->d_J,
+                  ctx->d_C, ctx->d_Cg, ctx->d_H, ctx->d_H2, ctx->d_Kpart, ctx->d_K,
+                  ctx->d_groups, ctx->d_tiles};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  for (auto& pe : ctx->pending) {
+    cudaEventDestroy(pe.second.first);
+    cudaEventDestroy(pe.second.second);
+  }
+  for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+const char* gbjk_last_error(const gbjk_ctx* ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+gbjk_status gbjk_upload_b(gbjk_ctx* ctx, const double* B) {
+  if (!ctx || !B) return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b: null argument");
+  CK(cudaSetDevice(ctx->device));
+  gbjk_status s;
+  if ((s = dalloc(ctx, &ctx->d_B, (size_t)ctx->nnz))) return s;
+  CK(cudaMemcpy(ctx->d_B, B, (size_t)ctx->nnz * sizeof(double), cudaMemcpyHostToDevice));
+  ctx->have_B = true;
+  ctx->ws_nocc = -1;  // plans hold d_B
+  ctx->split.invalidate_b();
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* Vinv) {
+  if (!ctx || !Linv || !Vinv) return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_metric: null argument");
+  CK(cudaSetDevice(ctx->device));
+  const size_t n2 = (size_t)ctx->naux * ctx->naux;
+  gbjk_status s;
+  if ((s = dalloc(ctx, &ctx->d_Linv, n2)) || (s = dalloc(ctx, &ctx->d_Vinv, n2))) return s;
+  CK(cudaMemcpy(ctx->d_Linv, Linv, n2 * sizeof(double), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_Vinv, Vinv, n2 * sizeof(double), cudaMemcpyHostToDevice));
+  ctx->have_metric = true;
+  ctx->ws_nocc = -1;
+  ctx->split.invalidate_b();
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (precision != GBJK_FP64 && precision != GBJK_SPLIT_BF16)
+    return fail(ctx, GBJK_INVALID_ARG, "unknown precision");
+  if (nslices < 0 || nslices > kMaxSlices)
+    return fail(ctx, GBJK_INVALID_ARG, "nslices out of range");
+  ctx->precision = precision;
+  ctx->nslices = nslices;
+  return GBJK_OK;
+}
+
+static gbjk_status check_ready(gbjk_ctx* ctx) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (!ctx->have_B || !ctx->have_metric)
+    return fail(ctx, GBJK_NOT_READY, "3-center tensor and metric must be uploaded first");
+  if (cudaSetDevice(ctx->device) != cudaSuccess)
+    return fail(ctx, GBJK_CUDA_ERROR, "cudaSetDevice failed");
+  return GBJK_OK;
+}
+
+static gbjk_status prepare_split(gbjk_ctx* ctx, int nocc) {
+  if (ctx->precision != GBJK_SPLIT_BF16) return GBJK_OK;
+  return ctx->split.prepare(ctx->stream, ctx->d_B, ctx->d_Linv, ctx->d_Vinv, ctx->d_Cg, nocc,
+                            ctx->nslices, &ctx->launches, &ctx->dev_bytes, &ctx->err);
+}
+
+gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, const double* dC,
+                                int nocc, double* dJ, double* dK) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (kmethod != GBJK_K_DFMO && kmethod != GBJK_K_DFLMO)
+    return fail(ctx, GBJK_INVALID_ARG, "Invalid kmethod");
+  if ((dK && (!dC || nocc <= 0)) || (dJ && !dP))
+    return fail(ctx, GBJK_INVALID_ARG, "missing density or coefficients");
+  if ((s = ensure_j_workspace(ctx))) return s;
+  if (dK) {
+    if ((s = ensure_k_workspace(ctx, nocc))) return s;
+    if ((s = prepare_split(ctx, nocc))) return s;
+  }
+  if (dJ && (s = run_j(ctx, dP, dJ))) return s;
+  if (dK && (s = run_k(ctx, kmethod, dC, nocc, dK))) return s;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_synchronize(gbjk_ctx* ctx) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  resolve_profile(ctx);
+  return GBJK_OK;
+}
+
+void* gbjk_stream(gbjk_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* P, const double* Cocc,
+                            int nocc, double* J, double* K) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if ((s = ensure_j_workspace(ctx))) return s;
+  const size_t n2 = (size_t)ctx->nbf * ctx->nbf;
+  if (K) {
+    if (!Cocc || nocc <= 0) return fail(ctx, GBJK_INVALID_ARG, "missing coefficients");
+    if ((s = ensure_k_workspace(ctx, nocc))) return s;
+    CK(cudaMemcpyAsync(ctx->d_C, Cocc, (size_t)ctx->nbf * nocc * sizeof(double),
+                       cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if (J) {
+    if (!P) return fail(ctx, GBJK_INVALID_ARG, "missing density");
+    CK(cudaMemcpyAsync(ctx->d_P, P, n2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  }
+  if ((s = gbjk_compute_jk_dev(ctx, kmethod, J ? ctx->d_P : nullptr, K ? ctx->d_C : nullptr,
+                               nocc, J ? ctx->d_J : nullptr, K ? ctx->d_K : nullptr)))
+    return s;
+  if (J) CK(cudaMemcpyAsync(J, ctx->d_J, n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (K) CK(cudaMemcpyAsync(K, ctx->d_K, n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  return gbjk_synchronize(ctx);
+}
+
+gbjk_status gbjk_compute_j(gbjk_ctx* ctx, const double* P, double* J) {
+  if (!P || !J) return fail(ctx, GBJK_INVALID_ARG, "gbjk_compute_j: null argument");
+  return gbjk_compute_jk(ctx, GBJK_K_DFMO, P, nullptr, 0, J, nullptr);
+}
+
+gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int nocc, double* K) {
+  if (!Cocc || !K) return fail(ctx, GBJK_INVALID_ARG, "gbjk_compute_k: null argument");
+  return gbjk_compute_jk(ctx, kmethod, nullptr, Cocc, nocc, nullptr, K);
+}
+
+size_t gbjk_device_bytes(const gbjk_ctx* ctx) { return ctx ? ctx->dev_bytes + ctx->split.bytes : 0; }
+int64_t gbjk_kernel_launches(const gbjk_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+gbjk_status gbjk_profile(gbjk_ctx* ctx, int enable) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  cudaStreamSynchronize(ctx->stream);
+  resolve_profile(ctx);
+  ctx->profile = enable != 0;
+  for (int i = 0; i < PH_COUNT; ++i) {
+    ctx->ph_ms[i] = 0;
+    ctx->ph_launch[i] = 0;
+  }
+  ctx->split.reset_profile();
+  return GBJK_OK;
+}
+
+int gbjk_profile_read(const gbjk_ctx* ctx, int idx, const char** name, double* ms,
+                      int64_t* launches) {
+  if (!ctx || idx < 0) return 0;
+  if (idx < PH_COUNT) {
+    if (name) *name = kPhaseNames[idx];
+    if (ms) *ms = ctx->ph_ms[idx];
+    if (launches) *launches = ctx->ph_launch[idx];
+    return 1;
+  }
+  return ctx->split.profile_read(idx - PH_COUNT, name, ms, launches);
+}
+
+}  // extern "C"

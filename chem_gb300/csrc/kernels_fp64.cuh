@@ -1,0 +1,224 @@
+// FP64 kernels of the DF J/K build (the plain path).
+//
+// The 3-center tensor lives in atom-block panels (see gbjk.h):
+//   panel I = [b_I][naux][K_I] FP64 at B + panel_off[I].
+// Every kernel is deterministic: each output element is produced by exactly
+// one thread (or one warp) with a fixed summation order, and cross-block
+// sums go through partial buffers reduced in a fixed order.
+#pragma once
+#include "common.cuh"
+
+namespace gbjk {
+
+// Pg[pg_off[I] + m*K_I + k] = P[(boff[I]+m)*ld + colmap[cmoff[I]+k]]
+// grid: (ceil(maxK/128), nbf); block 128.
+__global__ void k_gather_panel_rows(const double* __restrict__ P, int ld,
+                                    const int* __restrict__ blk_of, const int* __restrict__ boff,
+                                    const int* __restrict__ panel_K,
+                                    const long long* __restrict__ pg_off,
+                                    const int* __restrict__ cmoff, const int* __restrict__ colmap,
+                                    double* __restrict__ Pg) {
+  const int mu = blockIdx.y;
+  const int I = blk_of[mu];
+  const int m = mu - boff[I];
+  const int KI = panel_K[I];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= KI) return;
+  Pg[pg_off[I] + (long long)m * KI + k] = P[(long long)mu * ld + colmap[cmoff[I] + k]];
+}
+
+// Cg[r*n + i] = C[colmap[r]*n + i] for all panel columns r.
+__global__ void k_gather_cols(const double* __restrict__ Cm, int n, const int* __restrict__ colmap,
+                              int nrows, double* __restrict__ Cg) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long total = (long long)nrows * n;
+  if (idx >= total) return;
+  const int r = (int)(idx / n), i = (int)(idx % n);
+  Cg[idx] = Cm[(long long)colmap[r] * n + i];
+}
+
+// part[mu][X] = sum_k B_I[m][X][k] * Pg_I[m][k]; one warp per (mu, X) row.
+__global__ void k_j_rowdot(const double* __restrict__ B, const long long* __restrict__ panel_off,
+                           const int* __restrict__ blk_of, const int* __restrict__ boff,
+                           const int* __restrict__ panel_K, const long long* __restrict__ pg_off,
+                           const double* __restrict__ Pg, int nbf, int naux,
+                           double* __restrict__ part) {
+  const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= (long long)nbf * naux) return;
+  const int mu = (int)(row / naux), X = (int)(row % naux);
+  const int I = blk_of[mu];
+  const int m = mu - boff[I];
+  const int KI = panel_K[I];
+  const double* br = B + panel_off[I] + ((long long)m * naux + X) * KI;
+  const double* pr = Pg + pg_off[I] + (long long)m * KI;
+  double s = 0.0;
+  for (int k = lane; k < KI; k += 32) s = fma(br[k], pr[k], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) part[(long long)mu * naux + X] = s;
+}
+
+// g[X] = sum_{mu} part[mu][X] (fixed order).
+__global__ void k_reduce_rows(const double* __restrict__ part, int nrows, int ncols,
+                              double* __restrict__ g) {
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  if (X >= ncols) return;
+  double s = 0.0;
+  for (int r = 0; r < nrows; ++r) s += part[(long long)r * ncols + X];
+  g[X] = s;
+}
+
+// y = M x, M n x n row-major; one warp per row.
+__global__ void k_gemv(const double* __restrict__ M, const double* __restrict__ x, int n,
+                       double* __restrict__ y) {
+  const int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (row >= n) return;
+  const double* mr = M + (long long)row * n;
+  double s = 0.0;
+  for (int k = lane; k < n; k += 32) s = fma(mr[k], x[k], s);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) y[row] = s;
+}
+
+// J[mu][colmap[k]] = sum_X B_I[m][X][k] h[X]; grid (ceil(maxK/128), nbf).
+__global__ void k_j_colsum(const double* __restrict__ B, const long long* __restrict__ panel_off,
+                           const int* __restrict__ blk_of, const int* __restrict__ boff,
+                           const int* __restrict__ panel_K, const int* __restrict__ cmoff,
+                           const int* __restrict__ colmap, const double* __restrict__ h,
+                           int nbf, int naux, double* __restrict__ J) {
+  extern __shared__ double hs[];
+  for (int x = threadIdx.x; x < naux; x += blockDim.x) hs[x] = h[x];
+  __syncthreads();
+  const int mu = blockIdx.y;
+  const int I = blk_of[mu];
+  const int m = mu - boff[I];
+  const int KI = panel_K[I];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= KI) return;
+  const double* b = B + panel_off[I] + (long long)m * naux * KI + k;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int X = 0;
+  for (; X + 3 < naux; X += 4) {
+    s0 = fma(b[(long long)X * KI], hs[X], s0);
+    s1 = fma(b[(long long)(X + 1) * KI], hs[X + 1], s1);
+    s2 = fma(b[(long long)(X + 2) * KI], hs[X + 2], s2);
+    s3 = fma(b[(long long)(X + 3) * KI], hs[X + 3], s3);
+  }
+  for (; X < naux; ++X) s0 = fma(b[(long long)X * KI], hs[X], s0);
+  J[(long long)mu * nbf + colmap[cmoff[I] + k]] = (s0 + s1) + (s2 + s3);
+}
+
+// Grouped FP64 GEMM over a tile list; 64x64 tiles, 256 threads, 4x4 per thread.
+template <bool TRANSB>
+__global__ void __launch_bounds__(256)
+    k_gemm_fp64(const GemmGroup* __restrict__ groups, const GemmTile* __restrict__ tiles,
+                double alpha) {
+  __shared__ double As[16][65];
+  __shared__ double Bs[16][65];
+  const GemmTile t = tiles[blockIdx.x];
+  const GemmGroup g = groups[t.group];
+  const int tid = threadIdx.x;
+  const int tx = tid & 15, ty = tid >> 4;
+  const int m0 = t.mt * 64, n0 = t.nt * 64;
+  int kend = t.k1;
+  if ((g.flags & kLowerA) && kend > m0 + 64) kend = m0 + 64;  // A[m][k] = 0 for k > m
+  double acc[4][4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+#pragma unroll
+    for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
+  for (int k0 = t.k0; k0 < kend; k0 += 16) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + 256 * r;
+      const int row = idx >> 4, kk = idx & 15;
+      const int gm = m0 + row, gk = k0 + kk;
+      As[kk][row] = (gm < g.M && gk < kend) ? g.A[(long long)gm * g.lda + gk] : 0.0;
+    }
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int idx = tid + 256 * r;
+      if (TRANSB) {
+        const int col = idx >> 4, kk = idx & 15;
+        const int gn = n0 + col, gk = k0 + kk;
+        Bs[kk][col] = (gn < g.N && gk < kend) ? g.B[(long long)gn * g.ldb + gk] : 0.0;
+      } else {
+        const int kk = idx >> 6, col = idx & 63;
+        const int gn = n0 + col, gk = k0 + kk;
+        Bs[kk][col] = (gn < g.N && gk < kend) ? g.B[(long long)gk * g.ldb + gn] : 0.0;
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < 16; ++kk) {
+      double a[4], b[4];
+#pragma unroll
+      for (int r = 0; r < 4; ++r) a[r] = As[kk][ty + 16 * r];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) b[c] = Bs[kk][tx + 16 * c];
+#pragma unroll
+      for (int r = 0; r < 4; ++r)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) acc[r][c] = fma(a[r], b[c], acc[r][c]);
+    }
+    __syncthreads();
+  }
+  double* C = g.C + t.coff;
+#pragma unroll
+  for (int r = 0; r < 4; ++r) {
+    const int gm = m0 + ty + 16 * r;
+    if (gm >= g.M) continue;
+#pragma unroll
+    for (int c = 0; c < 4; ++c) {
+      const int gn = n0 + tx + 16 * c;
+      if (gn >= g.N) continue;
+      double v = alpha * acc[r][c];
+      if (g.flags & kAccum) v += C[(long long)gm * g.ldc + gn];
+      C[(long long)gm * g.ldc + gn] = v;
+    }
+  }
+}
+
+// out[m][n] = alpha * sum_s part[s][m][n] over the upper triangle (n >= m)
+// when symmetric (mirrored to the lower one), else everywhere.
+__global__ void k_splitk_reduce(const double* __restrict__ part, int nsplit, int n,
+                                double alpha, int symmetric, double* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * n) return;
+  const int m = (int)(idx / n), c = (int)(idx % n);
+  if (symmetric && c < m) return;
+  double s = 0.0;
+  for (int k = 0; k < nsplit; ++k) s += part[(long long)k * n * n + idx];
+  s *= alpha;
+  out[idx] = s;
+  if (symmetric && c != m) out[(long long)c * n + m] = s;
+}
+
+// Zero atom blocks (I, J) of the n x n matrix M with Frobenius norm < eps.
+// grid (nblk, nblk), block 128.
+__global__ void k_block_filter(double* __restrict__ M, int n, const int* __restrict__ boff,
+                               double eps) {
+  const int I = blockIdx.x, J = blockIdx.y;
+  const int r0 = boff[I], nr = boff[I + 1] - r0;
+  const int c0 = boff[J], nc = boff[J + 1] - c0;
+  __shared__ double red[128];
+  double s = 0.0;
+  for (int e = threadIdx.x; e < nr * nc; e += blockDim.x) {
+    const double v = M[(long long)(r0 + e / nc) * n + c0 + e % nc];
+    s = fma(v, v, s);
+  }
+  red[threadIdx.x] = s;
+  __syncthreads();
+  for (int o = 64; o > 0; o >>= 1) {
+    if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+    __syncthreads();
+  }
+  if (sqrt(red[0]) < eps)
+    for (int e = threadIdx.x; e < nr * nc; e += blockDim.x)
+      M[(long long)(r0 + e / nc) * n + c0 + e % nc] = 0.0;
+}
+
+}  // namespace gbjk

@@ -1,0 +1,288 @@
+"""J/K builders over the GB300 engine (libgbjk.so, include/gbjk.h).
+
+Mirrors megalochem's builder interface (src/fock/jkbuilder.hpp:62-210):
+abstract J and K classes with set_density_alpha/beta, set_coeff_alpha/beta,
+set_sym, set_SAD, init(), compute_J()/compute_K(), get_J()/get_K_A()/get_K_B(),
+and factories create_j()/create_k() keyed by the same method strings
+("dfao" for J; "dfmo", "dflmo" for K).  Errors raise RuntimeError with the
+engine's message, as the reference throws std::runtime_error.
+
+All arithmetic runs in the CUDA library; this module only moves host arrays
+across the C ABI.  There is no CPU fallback: without the built library (or a
+GPU) every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_LIBDIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib")
+_lib = None
+
+GBJK_FP64 = 0
+GBJK_SPLIT_BF16 = 1
+KMETHODS = {"dfmo": 0, "dflmo": 1}
+JMETHODS = ("dfao",)
+STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT",
+          5: "NOT_CONVERGED", 6: "NOT_READY"}
+
+
+class GbjkDesc(C.Structure):
+    _fields_ = [("nbf", C.c_int), ("naux", C.c_int), ("nblk", C.c_int),
+                ("blk_size", C.POINTER(C.c_int)), ("panel_K", C.POINTER(C.c_int)),
+                ("colmap", C.POINTER(C.c_int)), ("filter_eps", C.c_double), ("device", C.c_int)]
+
+
+def lib_path():
+    return os.path.join(_LIBDIR, "libgbjk.so")
+
+
+def lib():
+    """Load libgbjk.so; raises if it was not built (no fallback)."""
+    global _lib
+    if _lib is None:
+        path = lib_path()
+        if not os.path.exists(path):
+            raise RuntimeError(f"{path} missing: the CUDA engine is not built "
+                               "(run __graft_entry__.build())")
+        L = C.CDLL(path)
+        vp, dp = C.c_void_p, C.POINTER(C.c_double)
+        L.gbjk_create.argtypes = [C.POINTER(vp), C.POINTER(GbjkDesc)]
+        L.gbjk_destroy.argtypes = [vp]
+        L.gbjk_last_error.argtypes = [vp]
+        L.gbjk_last_error.restype = C.c_char_p
+        L.gbjk_upload_b.argtypes = [vp, dp]
+        L.gbjk_upload_metric.argtypes = [vp, dp, dp]
+        L.gbjk_set_precision.argtypes = [vp, C.c_int, C.c_int]
+        L.gbjk_compute_j.argtypes = [vp, dp, dp]
+        L.gbjk_compute_k.argtypes = [vp, C.c_int, dp, C.c_int, dp]
+        L.gbjk_compute_jk.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, dp]
+        L.gbjk_compute_jk_dev.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                          C.c_void_p, C.c_void_p]
+        L.gbjk_synchronize.argtypes = [vp]
+        L.gbjk_stream.argtypes = [vp]
+        L.gbjk_stream.restype = C.c_void_p
+        L.gbjk_device_bytes.argtypes = [vp]
+        L.gbjk_device_bytes.restype = C.c_size_t
+        L.gbjk_kernel_launches.argtypes = [vp]
+        L.gbjk_kernel_launches.restype = C.c_int64
+        L.gbjk_k_split_plan.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
+                                         C.POINTER(C.c_longlong)]
+        L.gbjk_profile.argtypes = [vp, C.c_int]
+        L.gbjk_profile_read.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), dp,
+                                        C.POINTER(C.c_int64)]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def k_split_plan(nbf, naux, nocc):
+    """(ksplit, kchunk) of the device exchange contraction (gbjk_k_split_plan)."""
+    ks = C.c_int()
+    kc = C.c_longlong()
+    if lib().gbjk_k_split_plan(nbf, naux, nocc, C.byref(ks), C.byref(kc)) != 0:
+        raise RuntimeError("gbjk_k_split_plan: invalid arguments")
+    return ks.value, kc.value
+
+
+class JKEngine:
+    """One gbjk context: the resident 3-center tensor and metric of a molecule."""
+
+    def __init__(self, layout, B, Linv, Vinv, eps=0.0, device=0, precision=GBJK_FP64,
+                 nslices=0):
+        L = lib()
+        self.layout = layout
+        self.nbf, self.naux = layout.nbf, layout.naux
+        cm = layout.column_map()
+        self._bs = np.ascontiguousarray(layout.bsizes, np.int32)
+        self._K = np.ascontiguousarray(layout.panel_K, np.int32)
+        self._cm = np.ascontiguousarray(np.concatenate(cm), np.int32)
+        desc = GbjkDesc(self.nbf, self.naux, layout.nblk,
+                        self._bs.ctypes.data_as(C.POINTER(C.c_int)),
+                        self._K.ctypes.data_as(C.POINTER(C.c_int)),
+                        self._cm.ctypes.data_as(C.POINTER(C.c_int)), float(eps), int(device))
+        h = C.c_void_p()
+        rc = L.gbjk_create(C.byref(h), C.byref(desc))
+        if rc != 0:
+            raise RuntimeError(f"gbjk_create failed: {STATUS.get(rc, rc)}")
+        self.h = h
+        B = np.ascontiguousarray(B, float)
+        if B.size != layout.nnz:
+            raise ValueError("B does not match the layout")
+        self._check(L.gbjk_upload_b(h, _dp(B)), "gbjk_upload_b")
+        self._check(L.gbjk_upload_metric(h, _dp(np.ascontiguousarray(Linv, float)),
+                                         _dp(np.ascontiguousarray(Vinv, float))),
+                    "gbjk_upload_metric")
+        self.set_precision(precision, nslices)
+
+    def _check(self, rc, what):
+        if rc != 0:
+            msg = lib().gbjk_last_error(self.h).decode()
+            raise RuntimeError(f"{what}: {STATUS.get(rc, rc)}: {msg}")
+
+    def set_precision(self, precision, nslices=0):
+        if isinstance(precision, str):
+            precision = {"fp64": GBJK_FP64, "split": GBJK_SPLIT_BF16,
+                         "split_bf16": GBJK_SPLIT_BF16}[precision]
+        self._check(lib().gbjk_set_precision(self.h, int(precision), int(nslices)),
+                    "gbjk_set_precision")
+        self.precision = precision
+
+    def compute_jk(self, Ptot=None, Cocc=None, kmethod="dfmo"):
+        n = self.nbf
+        J = np.zeros((n, n)) if Ptot is not None else None
+        K = np.zeros((n, n)) if Cocc is not None else None
+        P = np.ascontiguousarray(Ptot, float) if Ptot is not None else None
+        Cm = np.ascontiguousarray(Cocc, float) if Cocc is not None else None
+        nocc = Cm.shape[1] if Cm is not None else 0
+        self._check(lib().gbjk_compute_jk(
+            self.h, KMETHODS[kmethod], _dp(P) if P is not None else None,
+            _dp(Cm) if Cm is not None else None, nocc,
+            _dp(J) if J is not None else None, _dp(K) if K is not None else None),
+            "gbjk_compute_jk")
+        return J, K
+
+    def compute_jk_dev(self, dP, dC, nocc, dJ, dK, kmethod="dfmo"):
+        """Device pointers (ints); ordered on the engine stream, no sync."""
+        self._check(lib().gbjk_compute_jk_dev(self.h, KMETHODS[kmethod], dP, dC, int(nocc),
+                                              dJ, dK), "gbjk_compute_jk_dev")
+
+    def synchronize(self):
+        self._check(lib().gbjk_synchronize(self.h), "gbjk_synchronize")
+
+    @property
+    def stream(self):
+        return lib().gbjk_stream(self.h)
+
+    @property
+    def device_bytes(self):
+        return int(lib().gbjk_device_bytes(self.h))
+
+    @property
+    def kernel_launches(self):
+        return int(lib().gbjk_kernel_launches(self.h))
+
+    def profile(self, enable=True):
+        self._check(lib().gbjk_profile(self.h, int(enable)), "gbjk_profile")
+
+    def profile_read(self):
+        out = {}
+        i = 0
+        name = C.c_char_p()
+        ms = C.c_double()
+        n = C.c_int64()
+        while lib().gbjk_profile_read(self.h, i, C.byref(name), C.byref(ms), C.byref(n)):
+            out[name.value.decode()] = (ms.value, n.value)
+            i += 1
+        return out
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().gbjk_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# --- builder classes with the reference's interface ------------------------
+
+class JK_common:
+    def __init__(self, engine: JKEngine):
+        self.engine = engine
+        self.m_p_A = self.m_p_B = self.m_c_A = self.m_c_B = None
+        self.m_sym = True
+        self.m_SAD_iter = False
+        self.m_SAD_rank = 0
+
+    def set_density_alpha(self, P):
+        self.m_p_A = P
+
+    def set_density_beta(self, P):
+        self.m_p_B = P
+
+    def set_coeff_alpha(self, Cm):
+        self.m_c_A = Cm
+
+    def set_coeff_beta(self, Cm):
+        self.m_c_B = Cm
+
+    def set_sym(self, sym):
+        self.m_sym = bool(sym)
+
+    def set_SAD(self, sad, rank):
+        self.m_SAD_iter, self.m_SAD_rank = bool(sad), int(rank)
+
+
+class J(JK_common):
+    def init(self):
+        self.m_J = None
+
+    def get_J(self):
+        return self.m_J
+
+
+class K(JK_common):
+    def init(self):
+        self.m_K_A = self.m_K_B = None
+
+    def get_K_A(self):
+        return self.m_K_A
+
+    def get_K_B(self):
+        return self.m_K_B
+
+
+class DF_J(J):
+    """fock::DF_J (src/fock/jkdf.cpp:13-190): P_tot = 2 P_A (RHF) or P_A + P_B."""
+
+    def compute_J(self):
+        if self.m_p_A is None:
+            raise RuntimeError("DF_J: density not set")
+        Ptot = 2.0 * self.m_p_A if self.m_p_B is None else self.m_p_A + self.m_p_B
+        self.m_J, _ = self.engine.compute_jk(Ptot=Ptot)
+
+
+class _DFK(K):
+    kmethod = "dfmo"
+
+    def compute_K(self):
+        if self.m_c_A is None:
+            raise RuntimeError(f"{type(self).__name__}: coefficients not set")
+        _, self.m_K_A = self.engine.compute_jk(Cocc=self.m_c_A, kmethod=self.kmethod)
+        if self.m_c_B is not None:
+            _, self.m_K_B = self.engine.compute_jk(Cocc=self.m_c_B, kmethod=self.kmethod)
+
+
+class DFMO_K(_DFK):
+    """fock::DFMO_K (src/fock/jkdf.cpp:192-462)."""
+    kmethod = "dfmo"
+
+
+class DFLMO_K(_DFK):
+    """fock::DFLMO_K, symmetric branch (src/fock/jkdf.cpp:861-1091)."""
+    kmethod = "dflmo"
+
+
+def create_j(engine: JKEngine, method="dfao") -> J:
+    """fock::create_j (src/fock/jkbuilder.hpp:621-690)."""
+    if method not in JMETHODS:
+        raise RuntimeError("Invalid jmethod")
+    return DF_J(engine)
+
+
+def create_k(engine: JKEngine, method="dfmo") -> K:
+    """fock::create_k (src/fock/jkbuilder.hpp:698-841)."""
+    if method == "dfmo":
+        return DFMO_K(engine)
+    if method == "dflmo":
+        return DFLMO_K(engine)
+    raise RuntimeError("Invalid kmethod")

@@ -1,0 +1,106 @@
+"""Minimal closed-shell DF-HF SCF driver (FP64) around the J/K builders.
+
+Restates the parts of megalochem's hf::hfmod the configs need:
+  * Loewdin orthogonaliser X = S^-1/2 (src/math/linalg/orthogonalizer.cpp:14-45);
+  * form_fock: F = H + J + K_A with J from P_tot = 2 P_A and K_A already
+    negated (src/hf/hfscf.cpp:228-276);
+  * energy E = sum P_A (H + F) + E_nuc (src/hf/hfscf.cpp:278-296);
+  * error matrix FPS - SPF in the orthogonal basis and its RMS
+    (src/hf/hfscf.cpp:298-324, :381-384);
+  * DIIS extrapolation on the Fock matrices (src/math/solvers/diis.hpp:43-234);
+  * diagonalisation X^T F X and P = C_occ C_occ^T (src/hf/hfdiagfock.cpp:20-102).
+The guess is the core Hamiltonian (megalochem's default SAD guess runs an
+atomic UHF with exact J/K; the converged RHF state is the same).
+Diagonalisation, DIIS and the energy stay FP64 on the host; J and K come
+from the device engine.  With a split-precision engine the driver switches
+to the FP64 path once the DIIS error falls below `switch_thresh`.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class SCFResult:
+    energy: float
+    converged: bool
+    iterations: int
+    C: np.ndarray
+    eps: np.ndarray
+    P: np.ndarray
+    F: np.ndarray
+    history: list = field(default_factory=list)
+
+
+class DIIS:
+    """Pulay DIIS over (F, error) pairs (src/math/solvers/diis.hpp:43-234)."""
+
+    def __init__(self, max_vecs=8):
+        self.max_vecs = max_vecs
+        self.F, self.E = [], []
+
+    def push(self, F, err):
+        self.F.append(F.copy())
+        self.E.append(err.copy())
+        if len(self.F) > self.max_vecs:
+            self.F.pop(0)
+            self.E.pop(0)
+
+    def extrapolate(self):
+        n = len(self.F)
+        if n < 2:
+            return self.F[-1]
+        Bm = -np.ones((n + 1, n + 1))
+        Bm[n, n] = 0.0
+        for i in range(n):
+            for j in range(n):
+                Bm[i, j] = np.sum(self.E[i] * self.E[j])
+        rhs = np.zeros(n + 1)
+        rhs[n] = -1.0
+        c = np.linalg.lstsq(Bm, rhs, rcond=None)[0][:n]
+        return sum(ci * Fi for ci, Fi in zip(c, self.F))
+
+
+def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max_vecs=8,
+            switch=None, switch_thresh=1e-5, log=None):
+    """jk(P_alpha, C_occ) -> (J, K_alpha) with K already negated.
+    switch(): called once when the DIIS RMS error falls below switch_thresh
+    (moves a split-precision engine to FP64)."""
+    s, U = np.linalg.eigh(S)
+    X = U @ np.diag(s ** -0.5) @ U.T
+    F = Hcore.copy()
+    diis = DIIS(max_vecs)
+    E_old = 0.0
+    hist = []
+    switched = switch is None
+    for it in range(max_iter):
+        Fo = X.T @ F @ X
+        e, Cp = np.linalg.eigh(Fo)
+        Cm = X @ Cp
+        Cocc = Cm[:, :nocc]
+        P = Cocc @ Cocc.T
+        J, K = jk(P, Cocc)
+        F_new = Hcore + J + K
+        E = float(np.sum(P * (Hcore + F_new)) + enuc)
+        err = X.T @ (F_new @ P @ S - S @ P @ F_new) @ X
+        rms = float(np.sqrt(np.mean(err ** 2)))
+        hist.append((it, E, E - E_old, rms))
+        if log:
+            log(f"iter {it:3d}  E {E:.12f}  dE {E - E_old:.3e}  rms {rms:.3e}")
+        if not switched and rms < switch_thresh:
+            switch()
+            switched = True
+            E_old = E
+            F = F_new
+            continue
+        if it > 0 and abs(E - E_old) < conv and rms < np.sqrt(conv) and switched:
+            return SCFResult(E, True, it + 1, Cm, e, P, F_new, hist)
+        E_old = E
+        if it >= diis_start:
+            diis.push(F_new, err)
+            F = diis.extrapolate()
+        else:
+            F = F_new
+    return SCFResult(E, False, max_iter, Cm, e, P, F_new, hist)

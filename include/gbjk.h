@@ -1,0 +1,128 @@
+/* gbjk — GB300 engine for the density-fitted J/K (Fock) build.
+ *
+ * Drop-in replacement for the block-sparse contractions megalochem's DF J/K
+ * builders issue through DBCSR.  Each entry point stands in for a reference
+ * interface:
+ *
+ *   gbjk_create          fock::create_j()/create_k() ... .build() + init()
+ *                        (src/fock/jkbuilder.hpp:621-841,
+ *                         src/fock/jkcommon.cpp:18-57)
+ *   gbjk_upload_b        the aoloader registry entry key::dfit_coul_xbb /
+ *                        eri3c2e_batched handed to the builders
+ *                        (src/fock/jkbuilder.hpp:639-680,
+ *                         src/ints/aoloader.cpp:287-398)
+ *   gbjk_upload_metric   key::coul_xx_inv / key::coul_xx_invsqrt
+ *                        (src/ints/aoloader.cpp:164-183)
+ *   gbjk_compute_j       fock::DF_J::compute_J  (src/fock/jkdf.cpp:69-190)
+ *   gbjk_compute_k       fock::DFMO_K::compute_K (src/fock/jkdf.cpp:221-462),
+ *                        fock::DFLMO_K::compute_K (src/fock/jkdf.cpp:890-1091)
+ *   gbjk_compute_jk      hf::hfmod::form_fock's J + K calls
+ *                        (src/hf/hfscf.cpp:241-259)
+ *   gbjk_set_precision   no counterpart (precision selection of this engine)
+ *   gbjk_last_error      the what() of the std::runtime_error megalochem
+ *                        throws (src/fock/jkbuilder.hpp:58)
+ *
+ * Conventions: dense row-major FP64 nbf x nbf matrices (P, J, K) and
+ * nbf x nocc coefficient matrices at the boundary; block-sparse inside.
+ * Host-pointer calls copy in, compute and copy out before returning; *_dev
+ * variants take device pointers and are ordered on the context's stream.
+ * A context belongs to one host thread and one CUDA device.
+ */
+#ifndef GBJK_H
+#define GBJK_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GBJK_OK = 0,
+  GBJK_INVALID_ARG = 1,
+  GBJK_OOM = 2,
+  GBJK_CUDA_ERROR = 3,
+  GBJK_TIMEOUT = 4,
+  GBJK_NOT_CONVERGED = 5,
+  GBJK_NOT_READY = 6
+} gbjk_status;
+
+typedef enum { GBJK_FP64 = 0, GBJK_SPLIT_BF16 = 1 } gbjk_precision;
+
+/* K builder, by the reference's kmethod strings (src/fock/jkbuilder.hpp:37-60) */
+typedef enum { GBJK_K_DFMO = 0, GBJK_K_DFLMO = 1 } gbjk_kmethod;
+
+typedef struct gbjk_ctx gbjk_ctx;
+
+/* Atom-block panel layout of the 3-center tensor (X|mu nu):
+ * AO block I has blk_size[I] functions; panel I is the dense FP64 array
+ * [blk_size[I]][naux][panel_K[I]] and colmap lists, panel after panel, the
+ * AO index of each of its panel_K[I] columns.  Panels are stored back to
+ * back in block order. */
+typedef struct gbjk_desc {
+  int nbf;
+  int naux;
+  int nblk;
+  const int* blk_size;  /* nblk */
+  const int* panel_K;   /* nblk */
+  const int* colmap;    /* sum_I panel_K[I] */
+  double filter_eps;    /* result-block filter on J and K; 0 disables */
+  int device;           /* CUDA device ordinal */
+} gbjk_desc;
+
+gbjk_status gbjk_create(gbjk_ctx** ctx, const gbjk_desc* desc);
+void gbjk_destroy(gbjk_ctx* ctx);
+const char* gbjk_last_error(const gbjk_ctx* ctx);
+
+/* B: host FP64 panel array (sum_I blk_size[I]*naux*panel_K[I] doubles). */
+gbjk_status gbjk_upload_b(gbjk_ctx* ctx, const double* B);
+/* Linv: lower-triangular L^-1 with V = L L^T; Vinv = L^-T L^-1 (naux^2 each). */
+gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* Vinv);
+
+/* precision: GBJK_FP64 or GBJK_SPLIT_BF16; nslices = BF16 slices per FP64
+ * operand for the split path (ignored for FP64; 0 picks the default). */
+gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices);
+
+/* J_{mu nu} = sum_X (X|mu nu) [V^-1 g]_X, g_X = sum (X|mu nu) Ptot_{mu nu}. */
+gbjk_status gbjk_compute_j(gbjk_ctx* ctx, const double* Ptot, double* J);
+/* K_{mu nu} = -sum_{X,i} Bfit_{X mu i} Bfit_{X nu i}, Cocc is nbf x nocc. */
+gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int nocc, double* K);
+/* One Fock build: J from Ptot and K from Cocc in one call. */
+gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* Ptot, const double* Cocc,
+                            int nocc, double* J, double* K);
+
+/* Device-pointer variants, ordered on the context's stream (no host sync). */
+gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dPtot,
+                                const double* dCocc, int nocc, double* dJ, double* dK);
+gbjk_status gbjk_synchronize(gbjk_ctx* ctx);
+/* The context's cudaStream_t, as void*. */
+void* gbjk_stream(gbjk_ctx* ctx);
+
+/* Summation plan of the exchange contraction K = -sum_t A_mu,t B_nu,t over
+ * t < naux*nocc: the t range is cut into *ksplit chunks of *kchunk (the last
+ * one shorter), each summed in order, and the chunk sums are added in order.
+ * Needs no GPU; lets a checker reproduce the device's rounding exactly.
+ * No counterpart in the reference (DBCSR does not specify its order). */
+gbjk_status gbjk_k_split_plan(int nbf, int naux, int nocc, int* ksplit, long long* kchunk);
+
+/* Device memory held by the context, in bytes. */
+size_t gbjk_device_bytes(const gbjk_ctx* ctx);
+/* Kernels launched by this context since creation (for launch accounting). */
+int64_t gbjk_kernel_launches(const gbjk_ctx* ctx);
+
+/* Per-phase device time: enable != 0 starts recording CUDA events around
+ * every launch on the context's stream (and clears the totals);
+ * gbjk_profile_read(ctx, i, ...) returns 1 and the name, accumulated
+ * milliseconds and launch count of phase i, or 0 past the last phase.
+ * No counterpart in the reference (it times phases with util::mpi_time,
+ * src/utils/mpi_time.hpp:12-120). */
+gbjk_status gbjk_profile(gbjk_ctx* ctx, int enable);
+int gbjk_profile_read(const gbjk_ctx* ctx, int idx, const char** name, double* ms,
+                      int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBJK_H */

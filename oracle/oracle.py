@@ -1,0 +1,160 @@
+"""Python wrapper of the CPU oracle (dfjk_oracle.c) — TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+arm use this module, as the checker or the timed CPU baseline.  The product
+path (chem_gb300) never imports it.
+
+Parity unpinned: megalochem's J/K path cannot be built here (DBCSR, libcint,
+MPI, ScaLAPACK and HDF5 are absent) and it ships no golden outputs.  The C
+restatement is cross-checked against `dense_*` below, an independent numpy
+einsum of the same formulas over the dense tensor.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "build")
+SO = os.path.join(BUILD, "libdfjk_oracle.so")
+
+_lib = None
+
+
+class OracleLayout(C.Structure):
+    _fields_ = [
+        ("nbf", C.c_int), ("naux", C.c_int), ("nblk", C.c_int),
+        ("blk_off", C.POINTER(C.c_int)), ("panel_K", C.POINTER(C.c_int)),
+        ("panel_off", C.POINTER(C.c_longlong)), ("colmap_off", C.POINTER(C.c_int)),
+        ("colmap", C.POINTER(C.c_int)),
+    ]
+
+
+def build(force=False):
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "dfjk_oracle.c")
+    if force or not os.path.exists(SO) or os.path.getmtime(SO) < os.path.getmtime(src):
+        subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+                               "-std=c11", src, "-o", SO, "-lm"])
+    return SO
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(SO)
+        dp = C.POINTER(C.c_double)
+        lp = C.POINTER(OracleLayout)
+        L.oracle_df_j.argtypes = [lp, dp, dp, dp, dp, C.c_double]
+        L.oracle_dfmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
+        L.oracle_dflmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
+        L.oracle_dfao_k.argtypes = [lp, dp, dp, dp, dp, C.c_double]
+        L.oracle_half_transform.argtypes = [lp, dp, dp, C.c_int, dp]
+        L.oracle_filter.argtypes = [lp, dp, C.c_double]
+        _lib = L
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    """Holds a layout and the panel array; computes J/K on the CPU."""
+
+    def __init__(self, layout, B):
+        self.layout = layout
+        self.B = np.ascontiguousarray(B, float)
+        cm = layout.column_map()
+        self._blk_off = np.ascontiguousarray(layout.boff, np.int32)
+        self._K = np.ascontiguousarray(layout.panel_K, np.int32)
+        self._poff = np.ascontiguousarray(layout.panel_off, np.int64)
+        self._cmoff = np.ascontiguousarray(np.concatenate([[0], np.cumsum([len(c) for c in cm])]),
+                                           np.int32)
+        self._cm = np.ascontiguousarray(np.concatenate(cm) if cm else np.zeros(0), np.int32)
+        self.L = OracleLayout(layout.nbf, layout.naux, layout.nblk,
+                              self._blk_off.ctypes.data_as(C.POINTER(C.c_int)),
+                              self._K.ctypes.data_as(C.POINTER(C.c_int)),
+                              self._poff.ctypes.data_as(C.POINTER(C.c_longlong)),
+                              self._cmoff.ctypes.data_as(C.POINTER(C.c_int)),
+                              self._cm.ctypes.data_as(C.POINTER(C.c_int)))
+
+    def df_j(self, Vinv, Ptot, eps=0.0):
+        n = self.layout.nbf
+        J = np.zeros((n, n))
+        lib().oracle_df_j(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Vinv)),
+                          _dp(np.ascontiguousarray(Ptot)), _dp(J), eps)
+        return J
+
+    def dfmo_k(self, Linv, Cocc, eps=0.0, kchunk=0):
+        """kchunk: length of the in-order partial sums of the exchange
+        contraction (0 = one sum); the device path's value comes from
+        chem_gb300.fock.k_split_plan."""
+        n = self.layout.nbf
+        K = np.zeros((n, n))
+        Cocc = np.ascontiguousarray(Cocc, float)
+        rc = lib().oracle_dfmo_k(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Linv)),
+                                 _dp(Cocc), Cocc.shape[1], _dp(K), eps, int(kchunk))
+        if rc:
+            raise MemoryError("oracle_dfmo_k")
+        return K
+
+    def dflmo_k(self, Vinv, Cocc, eps=0.0, kchunk=0):
+        n = self.layout.nbf
+        K = np.zeros((n, n))
+        Cocc = np.ascontiguousarray(Cocc, float)
+        rc = lib().oracle_dflmo_k(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Vinv)),
+                                  _dp(Cocc), Cocc.shape[1], _dp(K), eps, int(kchunk))
+        if rc:
+            raise MemoryError("oracle_dflmo_k")
+        return K
+
+    def dfao_k(self, Vinv, P, eps=0.0):
+        n = self.layout.nbf
+        K = np.zeros((n, n))
+        rc = lib().oracle_dfao_k(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Vinv)),
+                                 _dp(np.ascontiguousarray(P)), _dp(K), eps)
+        if rc:
+            raise MemoryError("oracle_dfao_k")
+        return K
+
+    def half_transform(self, Cocc):
+        n, naux = self.layout.nbf, self.layout.naux
+        Cocc = np.ascontiguousarray(Cocc, float)
+        H = np.zeros((n, naux, Cocc.shape[1]))
+        lib().oracle_half_transform(C.byref(self.L), _dp(self.B), _dp(Cocc), Cocc.shape[1], _dp(H))
+        return H
+
+    def filter(self, M, eps):
+        M = np.ascontiguousarray(M, float).copy()
+        lib().oracle_filter(C.byref(self.L), _dp(M), eps)
+        return M
+
+
+# --- independent dense restatements (numpy einsum) -------------------------
+
+def dense_j(T, Vinv, Ptot):
+    g = np.einsum("xmn,mn->x", T, Ptot)
+    return np.einsum("x,xmn->mn", Vinv @ g, T)
+
+
+def dense_dfmo_k(T, Linv, Cocc):
+    H = np.einsum("xmn,mi->xin", T, Cocc)
+    H2 = np.einsum("yx,xin->yin", Linv, H)
+    return -np.einsum("xim,xin->mn", H2, H2)
+
+
+def dense_dflmo_k(T, Vinv, Cocc):
+    H = np.einsum("xmn,ni->xmi", T, Cocc)
+    Hf = np.einsum("xy,ymi->xmi", Vinv, H)
+    return -np.einsum("xmi,xni->nm", H, Hf)
+
+
+def dense_dfao_k(T, Vinv, P):
+    cbar = np.einsum("xmn,nl->xml", T, P)
+    c = np.einsum("xy,yns->xns", Vinv, T)
+    return -np.einsum("xns,xms->mn", c, cbar)

@@ -1,0 +1,86 @@
+"""FP64 device path against the CPU oracle, through the C ABI.
+
+The oracle and the kernels share one summation order per contraction, so
+J and K must agree bit for bit (tolerance 0); the config-1 bar of 1e-12 max
+abs is asserted as well.  Marked gpu: needs a GB300."""
+import numpy as np
+import pytest
+
+from chem_gb300.fock import JKEngine, create_j, create_k, k_split_plan
+from oracle.oracle import Oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _orbitals(ds, seed=11):
+    rng = np.random.default_rng(seed)
+    return np.linalg.qr(rng.standard_normal((ds.nbf, ds.nbf)))[0][:, :ds.nocc]
+
+
+def _engine(ds, eps=1e-10):
+    return JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=eps)
+
+
+@pytest.mark.parametrize("sysname", ["water", "butane"])
+@pytest.mark.parametrize("kmethod", ["dfmo", "dflmo"])
+def test_fp64_bitwise_vs_oracle(sysname, kmethod, request):
+    ds = request.getfixturevalue(sysname)
+    eng = _engine(ds)
+    O = Oracle(ds.layout, ds.B)
+    C = _orbitals(ds)
+    P = C @ C.T
+    J, K = eng.compute_jk(2 * P, C, kmethod)
+    kc = k_split_plan(ds.nbf, ds.naux, ds.nocc)[1]
+    Jr = O.df_j(ds.Vinv, 2 * P, 1e-10)
+    if kmethod == "dfmo":
+        Kr = O.dfmo_k(np.tril(ds.Linv), C, 1e-10, kchunk=kc)
+    else:
+        Kr = O.dflmo_k(ds.Vinv, C, 1e-10, kchunk=kc)
+    assert np.abs(J - Jr).max() <= 1e-12
+    assert np.abs(K - Kr).max() <= 1e-12
+    assert np.array_equal(J, Jr)
+    assert np.array_equal(K, Kr)
+
+
+def test_deterministic_and_builders(water):
+    ds = water
+    eng = _engine(ds)
+    C = _orbitals(ds, 5)
+    P = C @ C.T
+    j = create_j(eng, "dfao")
+    j.set_density_alpha(P)
+    j.init()
+    j.compute_J()
+    k = create_k(eng, "dfmo")
+    k.set_coeff_alpha(C)
+    k.init()
+    k.compute_K()
+    J2, K2 = eng.compute_jk(2 * P, C)
+    assert np.array_equal(j.get_J(), J2)
+    assert np.array_equal(k.get_K_A(), K2)
+    with pytest.raises(RuntimeError):
+        create_k(eng, "nope")
+
+
+def test_nocc_change_and_errors(butane):
+    ds = butane
+    eng = _engine(ds)
+    O = Oracle(ds.layout, ds.B)
+    for nocc in (3, ds.nocc, 1):
+        C = _orbitals(ds)[:, :nocc]
+        _, K = eng.compute_jk(None, C)
+        kc = k_split_plan(ds.nbf, ds.naux, nocc)[1]
+        assert np.array_equal(K, O.dfmo_k(np.tril(ds.Linv), C, 1e-10, kchunk=kc))
+    with pytest.raises(RuntimeError):
+        eng.compute_jk(None, np.zeros((ds.nbf, 0)))
+
+
+def test_empty_filter_eps_zero(water):
+    ds = water
+    eng = _engine(ds, eps=0.0)
+    O = Oracle(ds.layout, ds.B)
+    C = _orbitals(ds)
+    J, K = eng.compute_jk(2 * C @ C.T, C)
+    kc = k_split_plan(ds.nbf, ds.naux, ds.nocc)[1]
+    assert np.array_equal(J, O.df_j(ds.Vinv, 2 * C @ C.T, 0.0))
+    assert np.array_equal(K, O.dfmo_k(np.tril(ds.Linv), C, 0.0, kchunk=kc))
