@@ -380,6 +380,8 @@ gbjk_status filter(gbjk_ctx* ctx, double* M) {
 
 gbjk_status run_j(gbjk_ctx* ctx, const double* dP, double* dJ) {
   const int nbf = ctx->nbf, naux = ctx->naux;
+  // blocks of screened (I, J) pairs are never written by the column sums
+  CK(cudaMemsetAsync(dJ, 0, (size_t)nbf * nbf * sizeof(double), ctx->stream));
   {
     PhaseScope ps(ctx, PH_GATHER);
     k_gather_panel_rows<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, 0, ctx->stream>>>(

@@ -39,3 +39,15 @@ def butane():
     s, x = geometry.alkane(4)
     mol = molecule_from_angstrom(s, x, "cc-pvdz", "cc-pvdz-jkfit")
     return build_dfsystem(mol, eps=1e-10)
+
+
+@pytest.fixture(scope="session")
+def decane():
+    """n-C10H22: the smallest alkane here with Schwarz-screened block pairs
+    (96.5 % of AO block pairs kept)."""
+    from chem_gb300 import geometry
+    from chem_gb300.dfsystem import build_dfsystem
+    from chem_gb300.molecule import molecule_from_angstrom
+    s, x = geometry.alkane(10)
+    mol = molecule_from_angstrom(s, x, "cc-pvdz", "cc-pvdz-jkfit")
+    return build_dfsystem(mol, eps=1e-10)

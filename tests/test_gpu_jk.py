@@ -21,7 +21,7 @@ def _engine(ds, eps=1e-10):
     return JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=eps)
 
 
-@pytest.mark.parametrize("sysname", ["water", "butane"])
+@pytest.mark.parametrize("sysname", ["water", "butane", "decane"])
 @pytest.mark.parametrize("kmethod", ["dfmo", "dflmo"])
 def test_fp64_bitwise_vs_oracle(sysname, kmethod, request):
     ds = request.getfixturevalue(sysname)
@@ -40,6 +40,13 @@ def test_fp64_bitwise_vs_oracle(sysname, kmethod, request):
     assert np.abs(K - Kr).max() <= 1e-12
     assert np.array_equal(J, Jr)
     assert np.array_equal(K, Kr)
+    if sysname == "decane":
+        # screened block pairs exist and come back as exact zeros
+        assert ds.layout.kept_block_fraction() < 1.0
+        I, Jb = next((i, j) for i in range(ds.layout.nblk) for j in range(ds.layout.nblk)
+                     if j not in ds.layout.nbr[i])
+        bo = ds.layout.boff
+        assert not J[bo[I]:bo[I + 1], bo[Jb]:bo[Jb + 1]].any()
 
 
 def test_deterministic_and_builders(water):
