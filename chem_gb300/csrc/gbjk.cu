@@ -15,6 +15,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <unordered_map>
@@ -721,3 +722,157 @@ int gbjk_profile_read(const gbjk_ctx* ctx, int idx, const char** name, double* m
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// DF-J without device allocation.
+//
+// Some callers cannot call cudaMalloc: code running inside a host framework
+// that owns all device memory through its own pool, or code that must not
+// allocate while a CUDA graph is being captured.  gbjk_compute_j_noalloc
+// runs the same J kernels as the context path, with every scratch buffer
+// (launch metadata, gathered density rows, per-row partial sums, g and h)
+// carved out of one file-scope device array of kNoallocScratchBytes.  The
+// module holds that array on every GPU that loads the library, until exit.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr size_t kNoallocScratchBytes = 16u << 20;  // 16 MiB
+constexpr int kNoallocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+// Device address of g_noalloc_scratch per device, looked up once per device.
+void* g_noalloc_ptr[kNoallocMaxDevices] = {};
+std::mutex g_noalloc_mu;
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Prefix sums of the layout inside the scratch array (one block).
+__global__ void k_noalloc_layout(int nbf, int naux, int nblk, const int* __restrict__ bsize,
+                                 const int* __restrict__ panelK, int* boff, int* cmoff,
+                                 long long* panel_off, long long* pg_off, int* blk_of) {
+  if (threadIdx.x == 0) {
+    int b = 0, c = 0;
+    long long po = 0, pg = 0;
+    for (int I = 0; I < nblk; ++I) {
+      boff[I] = b;
+      cmoff[I] = c;
+      panel_off[I] = po;
+      pg_off[I] = pg;
+      b += bsize[I];
+      c += panelK[I];
+      po += (long long)bsize[I] * naux * panelK[I];
+      pg += (long long)bsize[I] * panelK[I];
+    }
+    boff[nblk] = b;
+    cmoff[nblk] = c;
+  }
+  __syncthreads();
+  for (int I = 0; I < nblk; ++I)
+    for (int m = threadIdx.x; m < bsize[I]; m += blockDim.x) blk_of[boff[I] + m] = I;
+}
+
+}  // namespace
+
+extern "C" gbjk_status gbjk_compute_j_noalloc(const gbjk_desc* d, const int* d_colmap,
+                                              const double* d_B, const double* d_Vinv,
+                                              const double* d_Ptot, double* d_J, void* stream,
+                                              char* errbuf, size_t errlen) {
+  auto err = [&](gbjk_status s, const std::string& m) {
+    if (errbuf && errlen) {
+      std::snprintf(errbuf, errlen, "%s", m.c_str());
+    }
+    return s;
+  };
+  if (!d || !d->blk_size || !d->panel_K || !d_colmap || !d_B || !d_Vinv || !d_Ptot || !d_J)
+    return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: null argument");
+  const int nbf = d->nbf, naux = d->naux, nblk = d->nblk;
+  if (nbf <= 0 || naux <= 0 || nblk <= 0)
+    return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: sizes must be positive");
+  long long bsum = 0, pg_total = 0;
+  int maxK = 0;
+  for (int I = 0; I < nblk; ++I) {
+    if (d->blk_size[I] <= 0 || d->panel_K[I] < 0 || d->panel_K[I] > nbf)
+      return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: bad block size or panel width");
+    bsum += d->blk_size[I];
+    pg_total += (long long)d->blk_size[I] * d->panel_K[I];
+    maxK = std::max(maxK, d->panel_K[I]);
+  }
+  if (bsum != nbf) return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: block sizes != nbf");
+  if ((size_t)naux * sizeof(double) > 48 * 1024)
+    return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: naux > 6144 not supported");
+  // scratch layout
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    const size_t o = off;
+    off = align256(off + bytes);
+    return o;
+  };
+  const size_t o_bsize = take(sizeof(int) * nblk), o_panelK = take(sizeof(int) * nblk);
+  const size_t o_boff = take(sizeof(int) * (nblk + 1)), o_cmoff = take(sizeof(int) * (nblk + 1));
+  const size_t o_poff = take(sizeof(long long) * nblk), o_pgoff = take(sizeof(long long) * nblk);
+  const size_t o_blkof = take(sizeof(int) * nbf);
+  const size_t o_pg = take(sizeof(double) * (size_t)pg_total);
+  const size_t o_part = take(sizeof(double) * (size_t)nbf * naux);
+  const size_t o_g = take(sizeof(double) * naux), o_h = take(sizeof(double) * naux);
+  if (off > kNoallocScratchBytes)
+    return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: problem needs " + std::to_string(off) +
+                                     " scratch bytes, limit is " +
+                                     std::to_string(kNoallocScratchBytes) +
+                                     " (nbf*naux + sum b_I*K_I + 2*naux doubles + layout)");
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kNoallocMaxDevices)
+    return err(GBJK_CUDA_ERROR, "gbjk_compute_j_noalloc: no current device");
+  unsigned char* base;
+  {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p)
+        return err(GBJK_CUDA_ERROR, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+      g_noalloc_ptr[dev] = p;
+    }
+    base = (unsigned char*)g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  int* bsize = (int*)(base + o_bsize);
+  int* panelK = (int*)(base + o_panelK);
+  int* boff = (int*)(base + o_boff);
+  int* cmoff = (int*)(base + o_cmoff);
+  long long* poff = (long long*)(base + o_poff);
+  long long* pgoff = (long long*)(base + o_pgoff);
+  int* blk_of = (int*)(base + o_blkof);
+  double* Pg = (double*)(base + o_pg);
+  double* part = (double*)(base + o_part);
+  double* g = (double*)(base + o_g);
+  double* h = (double*)(base + o_h);
+  auto ck = [&](cudaError_t e, const char* what) {
+    return e == cudaSuccess ? GBJK_OK
+                            : err(GBJK_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
+  };
+  gbjk_status s;
+  if ((s = ck(cudaMemcpyAsync(bsize, d->blk_size, sizeof(int) * nblk, cudaMemcpyHostToDevice, st),
+              "copy block sizes")))
+    return s;
+  if ((s = ck(cudaMemcpyAsync(panelK, d->panel_K, sizeof(int) * nblk, cudaMemcpyHostToDevice, st),
+              "copy panel widths")))
+    return s;
+  k_noalloc_layout<<<1, 256, 0, st>>>(nbf, naux, nblk, bsize, panelK, boff, cmoff, poff, pgoff,
+                                      blk_of);
+  if ((s = ck(cudaGetLastError(), "layout kernel"))) return s;
+  if ((s = ck(cudaMemsetAsync(d_J, 0, sizeof(double) * (size_t)nbf * nbf, st), "clear J")))
+    return s;
+  k_gather_panel_rows<<<dim3(cdiv(std::max(maxK, 1), 128), nbf), 128, 0, st>>>(
+      d_Ptot, nbf, blk_of, boff, panelK, pgoff, cmoff, d_colmap, Pg);
+  k_j_rowdot<<<cdiv((long long)nbf * naux * 32, 256), 256, 0, st>>>(d_B, poff, blk_of, boff,
+                                                                     panelK, pgoff, Pg, nbf, naux,
+                                                                     part);
+  k_reduce_rows<<<cdiv(naux, 128), 128, 0, st>>>(part, nbf, naux, g);
+  k_gemv<<<cdiv((long long)naux * 32, 256), 256, 0, st>>>(d_Vinv, g, naux, h);
+  k_j_colsum<<<dim3(cdiv(std::max(maxK, 1), 128), nbf), 128, naux * sizeof(double), st>>>(
+      d_B, poff, blk_of, boff, panelK, cmoff, d_colmap, h, nbf, naux, d_J);
+  if (d->filter_eps > 0)
+    k_block_filter<<<dim3(nblk, nblk), 128, 0, st>>>(d_J, nbf, boff, d->filter_eps);
+  return ck(cudaGetLastError(), "J kernels");
+}

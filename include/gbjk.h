@@ -106,6 +106,29 @@ void* gbjk_stream(gbjk_ctx* ctx);
  * No counterpart in the reference (DBCSR does not specify its order). */
 gbjk_status gbjk_k_split_plan(int nbf, int naux, int nocc, int* ksplit, long long* kchunk);
 
+/* DF-J for callers that cannot allocate device memory — for example code
+ * embedded in a host framework that owns all GPU memory through its own
+ * pool, or code that must not allocate while a CUDA graph is captured.
+ * No counterpart in the reference; it is an addition of this engine.
+ *
+ * Computes the same J as gbjk_compute_j (same kernels, same summation order)
+ * without a context: the caller passes the layout (desc: host arrays
+ * blk_size and panel_K; desc->colmap is ignored), the panel column map
+ * d_colmap, the panels d_B, V^-1 d_Vinv and P_tot d_Ptot in device memory,
+ * and receives J in d_J (device, nbf x nbf), all ordered on `stream`.
+ * It calls no cudaMalloc/cudaFree and no allocating library routine: all
+ * scratch lives in one 16 MiB file-scope device array that every GPU
+ * loading the library holds until exit.  Problems whose scratch
+ * (nbf*naux + sum_I blk_size[I]*panel_K[I] + 2*naux doubles plus the layout
+ * arrays) exceeds 16 MiB, or with naux > 6144, are rejected with
+ * GBJK_INVALID_ARG and a message in errbuf.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  All calls share the array: calls
+ * whose work overlaps on the GPU race and corrupt each other's results. */
+gbjk_status gbjk_compute_j_noalloc(const gbjk_desc* desc, const int* d_colmap, const double* d_B,
+                                   const double* d_Vinv, const double* d_Ptot, double* d_J,
+                                   void* stream, char* errbuf, size_t errlen);
+
 /* Device memory held by the context, in bytes. */
 size_t gbjk_device_bytes(const gbjk_ctx* ctx);
 /* Kernels launched by this context since creation (for launch accounting). */
