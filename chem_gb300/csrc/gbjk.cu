@@ -24,7 +24,7 @@
 #include "common.cuh"
 #include "gbjk.h"
 #include "kernels_fp64.cuh"
-#include "split_gemm.cuh"
+#include "split_host.cuh"
 
 using namespace gbjk;
 
@@ -654,6 +654,12 @@ gbjk_status gbjk_synchronize(gbjk_ctx* ctx) {
   if (!ctx) return GBJK_INVALID_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
   resolve_profile(ctx);
+  if (ctx->precision == GBJK_SPLIT_BF16) {
+    const int code = ctx->split.read_error();
+    if (code != 0)
+      return fail(ctx, GBJK_TIMEOUT,
+                  "split GEMM: a pipeline wait timed out (code " + std::to_string(code) + ")");
+  }
   return GBJK_OK;
 }
 
@@ -701,6 +707,7 @@ gbjk_status gbjk_profile(gbjk_ctx* ctx, int enable) {
   cudaStreamSynchronize(ctx->stream);
   resolve_profile(ctx);
   ctx->profile = enable != 0;
+  ctx->split.profile = enable != 0;
   for (int i = 0; i < PH_COUNT; ++i) {
     ctx->ph_ms[i] = 0;
     ctx->ph_launch[i] = 0;
@@ -718,7 +725,7 @@ int gbjk_profile_read(const gbjk_ctx* ctx, int idx, const char** name, double* m
     if (launches) *launches = ctx->ph_launch[idx];
     return 1;
   }
-  return ctx->split.profile_read(idx - PH_COUNT, name, ms, launches);
+  return const_cast<gbjk_ctx*>(ctx)->split.profile_read(idx - PH_COUNT, name, ms, launches);
 }
 
 }  // extern "C"

@@ -1,0 +1,494 @@
+// Host side of the split-precision K path: operand preparation and launch
+// plans.
+//
+// Once per tensor upload:
+//   Bfit = L^-1 B per panel row block (FP64 grouped GEMM, temporary), its row
+//   exponents and slice images (the A operands of the half transform).
+// Per nocc: buffers and the two work lists (half transform, exchange).
+// Per build (stream-ordered, no host sync):
+//   C digits (B operand of every panel) -> split GEMM Hfit = Bfit C ->
+//   H digits -> split GEMM Kpart = Hfit Hfit^T (upper tiles, split-K) ->
+//   ordered reduce K = -sum Kpart.
+// With the fit folded into the tensor, DF-MO and DF-LMO compute the same
+// K = -(L^-1 B C)^T (L^-1 B C).
+#pragma once
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "kernels_fp64.cuh"
+#include "split_gemm.cuh"
+
+namespace gbjk {
+
+struct SplitState {
+  size_t bytes = 0;
+  int nbf = 0, naux = 0, nblk = 0;
+  std::vector<int> bsize, boff, panelK, cmoff;
+  std::vector<long long> panel_off;
+  bool b_ready = false;
+  int nocc = -1;
+  // A operands (static)
+  uint16_t* d_Aslices = nullptr;
+  std::vector<long long> a_off, eA_off;
+  std::vector<int> a_nrb, nkt;
+  int* d_eA = nullptr;
+  // per build
+  uint16_t* d_Cslices = nullptr;
+  std::vector<long long> c_off;
+  int c_nrb = 0;
+  int* d_eC = nullptr;
+  double* d_H = nullptr;
+  uint16_t* d_Hslices = nullptr;
+  int h_nrb = 0, h_nkt = 0;
+  int* d_eH = nullptr;
+  double* d_Kpart = nullptr;
+  int ksplit = 1;
+  SplitItem* d_items = nullptr;
+  int ht_nitems = 0, k_nitems = 0;
+  SplitJob* d_jobs = nullptr;  // [0..nblk): C jobs, [nblk]: H job
+  int c_maxthreads = 0, c_maxrows = 0;
+  long long h_threads = 0;
+  int* d_err = nullptr;
+  const double* d_Cg = nullptr;
+  int nsm = 148;
+  bool attr_set = false;
+  bool profile = false;
+  double ms[4] = {0, 0, 0, 0};
+  int64_t nl[4] = {0, 0, 0, 0};
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
+
+  void init(int nbf_, int naux_, int nblk_, const std::vector<int>& bs,
+            const std::vector<int>& bo, const std::vector<int>& pk, const std::vector<int>& cmo,
+            const std::vector<long long>& po) {
+    nbf = nbf_;
+    naux = naux_;
+    nblk = nblk_;
+    bsize = bs;
+    boff = bo;
+    panelK = pk;
+    cmoff = cmo;
+    panel_off = po;
+  }
+  template <class T>
+  cudaError_t alloc(T** p, size_t n) {
+    const size_t b = std::max<size_t>(n, 1) * sizeof(T);
+    cudaError_t e = cudaMalloc((void**)p, b);
+    if (e == cudaSuccess)
+      bytes += b;
+    else
+      cudaGetLastError();
+    return e;
+  }
+  template <class T>
+  void free_(T** p) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+  }
+  void release_build() {
+    free_(&d_Cslices);
+    free_(&d_eC);
+    free_(&d_H);
+    free_(&d_Hslices);
+    free_(&d_eH);
+    free_(&d_Kpart);
+    free_(&d_items);
+    free_(&d_jobs);
+    nocc = -1;
+  }
+  void release() {
+    release_build();
+    free_(&d_Aslices);
+    free_(&d_eA);
+    free_(&d_err);
+    for (auto& pe : pending) {
+      cudaEventDestroy(pe.second.first);
+      cudaEventDestroy(pe.second.second);
+    }
+    pending.clear();
+    b_ready = false;
+    bytes = 0;
+  }
+  void invalidate_b() { release(); }
+  void reset_profile() {
+    resolve();
+    for (int i = 0; i < 4; ++i) {
+      ms[i] = 0;
+      nl[i] = 0;
+    }
+  }
+  void resolve() {
+    for (auto& pe : pending) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, pe.second.first, pe.second.second) == cudaSuccess)
+        ms[pe.first] += t;
+      cudaEventDestroy(pe.second.first);
+      cudaEventDestroy(pe.second.second);
+    }
+    pending.clear();
+  }
+  int profile_read(int idx, const char** name, double* out_ms, int64_t* launches) {
+    static const char* names[4] = {"split_gemm_ht", "split_gemm_k", "split_digits", "prefit"};
+    if (idx < 0 || idx >= 4) return 0;
+    resolve();
+    if (name) *name = names[idx];
+    if (out_ms) *out_ms = ms[idx];
+    if (launches) *launches = nl[idx];
+    return 1;
+  }
+  struct Scope {
+    SplitState* s;
+    int ph;
+    cudaStream_t st;
+    cudaEvent_t a = nullptr, b = nullptr;
+    Scope(SplitState* s_, int p, cudaStream_t st_) : s(s_), ph(p), st(st_) {
+      if (s->profile) {
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, st);
+      }
+      s->nl[ph]++;
+    }
+    ~Scope() {
+      if (s->profile) {
+        cudaEventRecord(b, st);
+        s->pending.push_back({ph, {a, b}});
+      }
+    }
+  };
+
+  static int cdiv_(long long a, long long b) { return (int)((a + b - 1) / b); }
+
+  gbjk_status launch_gemm(cudaStream_t st, SplitItem* items, int n, int64_t* launches,
+                          std::string* err) {
+    if (n == 0) return GBJK_OK;
+    if (!attr_set) {
+      if (cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               kSmemBytes) != cudaSuccess) {
+        *err = "cannot reserve shared memory for the split GEMM";
+        return GBJK_CUDA_ERROR;
+      }
+      int dev = 0;
+      cudaGetDevice(&dev);
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+      attr_set = true;
+    }
+    const int grid = std::min(n, nsm);
+    k_split_gemm<<<grid, kThreads, kSmemBytes, st>>>(items, n, d_err);
+    (*launches)++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      *err = std::string("split GEMM launch: ") + cudaGetErrorString(e);
+      return GBJK_CUDA_ERROR;
+    }
+    return GBJK_OK;
+  }
+
+  // --- once per tensor: prefit and A-operand digits -----------------------
+  gbjk_status prepare_b(cudaStream_t st, const double* d_B, const double* d_Linv,
+                        int64_t* launches, std::string* err) {
+    const long long nnz = panel_off.back() + (long long)bsize.back() * naux * panelK.back();
+    double* d_Bfit = nullptr;
+    if (alloc(&d_err, 1) != cudaSuccess || cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) {
+      *err = "split path: cannot allocate the error flag";
+      return GBJK_OOM;
+    }
+    if (alloc(&d_Bfit, (size_t)nnz) != cudaSuccess) {
+      *err = "split path: out of memory for the prefitted tensor";
+      return GBJK_OOM;
+    }
+    // Bfit_I[m] = L^-1 B_I[m]  (naux x K_I per AO function m)
+    std::vector<GemmGroup> groups;
+    std::vector<GemmTile> tiles;
+    for (int I = 0; I < nblk; ++I) {
+      const int K = panelK[I];
+      if (K == 0) continue;
+      for (int m = 0; m < bsize[I]; ++m) {
+        GemmGroup g;
+        const long long off = panel_off[I] + (long long)m * naux * K;
+        g.A = d_Linv;
+        g.B = d_B + off;
+        g.C = d_Bfit + off;
+        g.M = naux;
+        g.N = K;
+        g.K = naux;
+        g.lda = naux;
+        g.ldb = K;
+        g.ldc = K;
+        g.flags = kLowerA;
+        for (int mt = 0; mt < cdiv_(naux, 64); ++mt)
+          for (int nt = 0; nt < cdiv_(K, 64); ++nt)
+            tiles.push_back({(int)groups.size(), mt, nt, 0, naux, 0});
+        groups.push_back(g);
+      }
+    }
+    GemmGroup* dg = nullptr;
+    GemmTile* dt = nullptr;
+    if (alloc(&dg, groups.size()) != cudaSuccess || alloc(&dt, tiles.size()) != cudaSuccess) {
+      free_(&dg);
+      free_(&d_Bfit);
+      *err = "split path: out of memory for the prefit plan";
+      return GBJK_OOM;
+    }
+    cudaMemcpy(dg, groups.data(), groups.size() * sizeof(GemmGroup), cudaMemcpyHostToDevice);
+    cudaMemcpy(dt, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice);
+    {
+      Scope sc(this, 3, st);
+      // the grid limit is 2^31-1 blocks; launch in slices of 1M tiles
+      for (size_t t0 = 0; t0 < tiles.size(); t0 += (1u << 20)) {
+        const int n = (int)std::min<size_t>(1u << 20, tiles.size() - t0);
+        k_gemm_fp64<false><<<n, 256, 0, st>>>(dg, dt + t0, 1.0);
+        (*launches)++;
+      }
+    }
+    // A operands: rows (m, Y) of panel I, columns k
+    a_off.assign(nblk, 0);
+    eA_off.assign(nblk, 0);
+    a_nrb.assign(nblk, 0);
+    nkt.assign(nblk, 0);
+    long long atot = 0, etot = 0;
+    for (int I = 0; I < nblk; ++I) {
+      const long long rows = (long long)bsize[I] * naux;
+      a_nrb[I] = cdiv_(rows, kTileM) * (kTileM / 32);
+      nkt[I] = std::max(1, cdiv_(panelK[I], kTileK));
+      a_off[I] = atot;
+      eA_off[I] = etot;
+      atot += (long long)a_nrb[I] * nkt[I] * kSlices * kImage;
+      etot += (long long)a_nrb[I] * 32;
+    }
+    if (alloc(&d_Aslices, (size_t)atot) != cudaSuccess || alloc(&d_eA, (size_t)etot) != cudaSuccess) {
+      free_(&dg);
+      free_(&dt);
+      free_(&d_Bfit);
+      *err = "split path: out of memory for the operand digits";
+      return GBJK_OOM;
+    }
+    std::vector<SplitJob> jobs(nblk);
+    int maxrows = 0;
+    long long maxthr = 0;
+    for (int I = 0; I < nblk; ++I) {
+      SplitJob& j = jobs[I];
+      j.src = d_Bfit + panel_off[I];
+      j.rs = panelK[I];
+      j.cs = 1;
+      j.nrows = bsize[I] * naux;
+      j.ncols = panelK[I];
+      j.e = d_eA + eA_off[I];
+      j.nrb = a_nrb[I];
+      j.nkt = nkt[I];
+      j.dst = d_Aslices + a_off[I];
+      maxrows = std::max(maxrows, j.nrb * 32);
+      maxthr = std::max(maxthr, (long long)j.nrb * 32 * j.nkt * 4);
+    }
+    SplitJob* dj = nullptr;
+    if (alloc(&dj, jobs.size()) != cudaSuccess) {
+      *err = "split path: out of memory";
+      return GBJK_OOM;
+    }
+    cudaMemcpy(dj, jobs.data(), jobs.size() * sizeof(SplitJob), cudaMemcpyHostToDevice);
+    {
+      Scope sc(this, 2, st);
+      k_row_maxexp<<<dim3(cdiv_((long long)maxrows * 32, 256), nblk), 256, 0, st>>>(dj);
+      k_split_tiles<<<dim3(cdiv_(maxthr, 256), nblk), 256, 0, st>>>(dj);
+      *launches += 2;
+    }
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaFree(dj);
+    cudaFree(dg);
+    cudaFree(dt);
+    cudaFree(d_Bfit);
+    bytes -= (size_t)nnz * sizeof(double);
+    if (e != cudaSuccess) {
+      *err = std::string("split path preparation: ") + cudaGetErrorString(e);
+      return GBJK_CUDA_ERROR;
+    }
+    b_ready = true;
+    return GBJK_OK;
+  }
+
+  // --- per nocc: buffers and work lists ------------------------------------
+  gbjk_status prepare_nocc(cudaStream_t st, int nocc_, std::string* err) {
+    release_build();
+    const int ntn = cdiv_(nocc_, kTileN);
+    c_nrb = ntn * (kTileN / 32);
+    c_off.assign(nblk, 0);
+    long long ctot = 0;
+    for (int I = 0; I < nblk; ++I) {
+      c_off[I] = ctot;
+      ctot += (long long)c_nrb * nkt[I] * kSlices * kImage;
+    }
+    const long long hk = (long long)naux * nocc_;
+    h_nkt = cdiv_(hk, kTileK);
+    h_nrb = std::max(cdiv_(nbf, kTileM) * (kTileM / 32), cdiv_(nbf, kTileN) * (kTileN / 32));
+    const int kt_per = 256;  // at most 8192 k per exchange item
+    ksplit = cdiv_(h_nkt, kt_per);
+    if (alloc(&d_Cslices, (size_t)ctot) != cudaSuccess ||
+        alloc(&d_eC, (size_t)nblk * c_nrb * 32) != cudaSuccess ||
+        alloc(&d_H, (size_t)nbf * hk) != cudaSuccess ||
+        alloc(&d_Hslices, (size_t)h_nrb * h_nkt * kSlices * kImage) != cudaSuccess ||
+        alloc(&d_eH, (size_t)h_nrb * 32) != cudaSuccess ||
+        alloc(&d_Kpart, (size_t)ksplit * nbf * nbf) != cudaSuccess) {
+      release_build();
+      *err = "split path: out of memory for the per-build buffers";
+      return GBJK_OOM;
+    }
+    std::vector<SplitItem> items;
+    // half transform: Hfit rows (m, Y) of panel I, columns i
+    for (int I = 0; I < nblk; ++I) {
+      const long long rows = (long long)bsize[I] * naux;
+      for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
+        for (int nt = 0; nt < ntn; ++nt) {
+          SplitItem w;
+          w.a = d_Aslices + a_off[I];
+          w.a_nrb = a_nrb[I];
+          w.a_rb0 = mt * (kTileM / 32);
+          w.b = d_Cslices + c_off[I];
+          w.b_nrb = c_nrb;
+          w.b_rb0 = nt * (kTileN / 32);
+          w.kt0 = 0;
+          w.nkt = nkt[I];
+          w.ea = d_eA + eA_off[I] + (long long)mt * kTileM;
+          w.eb = d_eC + (long long)I * c_nrb * 32 + (long long)nt * kTileN;
+          w.out = d_H + ((long long)boff[I] * naux + (long long)mt * kTileM) * nocc_ +
+                  (long long)nt * kTileN;
+          w.ldr = nocc_;
+          w.m_valid = (int)std::min<long long>(kTileM, rows - (long long)mt * kTileM);
+          w.n_valid = std::min(kTileN, nocc_ - nt * kTileN);
+          items.push_back(w);
+        }
+    }
+    ht_nitems = (int)items.size();
+    // exchange: upper tiles, split over k
+    for (int ks = 0; ks < ksplit; ++ks) {
+      const int kt0 = ks * kt_per;
+      const int n_kt = std::min(kt_per, h_nkt - kt0);
+      for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
+        for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt) {
+          if ((nt + 1) * kTileN <= mt * kTileM) continue;  // strictly below the diagonal
+          SplitItem w;
+          w.a = d_Hslices;
+          w.a_nrb = h_nrb;
+          w.a_rb0 = mt * (kTileM / 32);
+          w.b = d_Hslices;
+          w.b_nrb = h_nrb;
+          w.b_rb0 = nt * (kTileN / 32);
+          w.kt0 = kt0;
+          w.nkt = n_kt;
+          w.ea = d_eH + (long long)mt * kTileM;
+          w.eb = d_eH + (long long)nt * kTileN;
+          w.out = d_Kpart + (long long)ks * nbf * nbf + (long long)mt * kTileM * nbf +
+                  (long long)nt * kTileN;
+          w.ldr = nbf;
+          w.m_valid = std::min(kTileM, nbf - mt * kTileM);
+          w.n_valid = std::min(kTileN, nbf - nt * kTileN);
+          items.push_back(w);
+        }
+    }
+    k_nitems = (int)items.size() - ht_nitems;
+    std::vector<SplitJob> jobs(nblk + 1);
+    c_maxthreads = 0;
+    c_maxrows = c_nrb * 32;
+    for (int I = 0; I < nblk; ++I) {
+      SplitJob& j = jobs[I];
+      j.src = nullptr;  // set per build (Cg pointer owned by the context)
+      j.rs = 1;
+      j.cs = nocc_;
+      j.nrows = nocc_;
+      j.ncols = panelK[I];
+      j.e = d_eC + (long long)I * c_nrb * 32;
+      j.nrb = c_nrb;
+      j.nkt = nkt[I];
+      j.dst = d_Cslices + c_off[I];
+      c_maxthreads = std::max(c_maxthreads, c_nrb * 32 * nkt[I] * 4);
+    }
+    SplitJob& hj = jobs[nblk];
+    hj.src = d_H;
+    hj.rs = hk;
+    hj.cs = 1;
+    hj.nrows = nbf;
+    hj.ncols = hk;
+    hj.e = d_eH;
+    hj.nrb = h_nrb;
+    hj.nkt = h_nkt;
+    hj.dst = d_Hslices;
+    h_threads = (long long)h_nrb * 32 * h_nkt * 4;
+    if (alloc(&d_items, items.size()) != cudaSuccess || alloc(&d_jobs, jobs.size()) != cudaSuccess) {
+      release_build();
+      *err = "split path: out of memory for the work lists";
+      return GBJK_OOM;
+    }
+    cudaMemcpy(d_items, items.data(), items.size() * sizeof(SplitItem), cudaMemcpyHostToDevice);
+    host_jobs = jobs;
+    nocc = nocc_;
+    (void)st;
+    return GBJK_OK;
+  }
+  std::vector<SplitJob> host_jobs;
+  const double* jobs_cg = nullptr;
+
+  gbjk_status prepare(cudaStream_t st, const double* d_B, const double* d_Linv,
+                      const double* /*d_Vinv*/, const double* d_Cg_, int nocc_, int /*nslices*/,
+                      int64_t* launches, size_t* /*dev_bytes*/, std::string* err) {
+    gbjk_status s;
+    if (!b_ready && (s = prepare_b(st, d_B, d_Linv, launches, err))) return s;
+    if (nocc != nocc_ && (s = prepare_nocc(st, nocc_, err))) return s;
+    if (jobs_cg != d_Cg_) {
+      for (int I = 0; I < nblk; ++I) host_jobs[I].src = d_Cg_ + (long long)cmoff[I] * nocc_;
+      if (cudaMemcpy(d_jobs, host_jobs.data(), host_jobs.size() * sizeof(SplitJob),
+                     cudaMemcpyHostToDevice) != cudaSuccess) {
+        *err = "split path: job upload failed";
+        return GBJK_CUDA_ERROR;
+      }
+      jobs_cg = d_Cg_;
+    }
+    return GBJK_OK;
+  }
+
+  // --- per build ------------------------------------------------------------
+  gbjk_status run_k(cudaStream_t st, double* dK, int64_t* launches, std::string* err) {
+    gbjk_status s;
+    {
+      Scope sc(this, 2, st);
+      k_row_maxexp<<<dim3(cdiv_((long long)c_maxrows * 32, 256), nblk), 256, 0, st>>>(d_jobs);
+      k_split_tiles<<<dim3(cdiv_(c_maxthreads, 256), nblk), 256, 0, st>>>(d_jobs);
+      *launches += 2;
+    }
+    {
+      Scope sc(this, 0, st);
+      if ((s = launch_gemm(st, d_items, ht_nitems, launches, err))) return s;
+    }
+    {
+      Scope sc(this, 2, st);
+      k_row_maxexp<<<dim3(cdiv_((long long)h_nrb * 32 * 32, 256), 1), 256, 0, st>>>(d_jobs + nblk);
+      k_split_tiles<<<dim3(cdiv_(h_threads, 256), 1), 256, 0, st>>>(d_jobs + nblk);
+      *launches += 2;
+    }
+    {
+      Scope sc(this, 1, st);
+      if ((s = launch_gemm(st, d_items + ht_nitems, k_nitems, launches, err))) return s;
+    }
+    k_splitk_reduce<<<cdiv_((long long)nbf * nbf, 256), 256, 0, st>>>(d_Kpart, ksplit, nbf, -1.0,
+                                                                      1, dK);
+    (*launches)++;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      *err = std::string("split path launch: ") + cudaGetErrorString(e);
+      return GBJK_CUDA_ERROR;
+    }
+    return GBJK_OK;
+  }
+
+  // error code recorded by a timed-out wait inside the split GEMM (0 = none)
+  int read_error() {
+    int h = 0;
+    if (d_err) cudaMemcpy(&h, d_err, sizeof(int), cudaMemcpyDeviceToHost);
+    return h;
+  }
+};
+
+inline gbjk_status split_run_k(SplitState& S, cudaStream_t st, int /*kmethod*/, int /*nocc*/,
+                               double* dK, int64_t* launches, std::string* err) {
+  return S.run_k(st, dK, launches, err);
+}
+
+}  // namespace gbjk
