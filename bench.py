@@ -35,7 +35,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--precision", default="split", choices=["fp64", "split"])
+    ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--alkane", type=int, default=20)
     ap.add_argument("--kmethod", default="dfmo")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -259,19 +260,33 @@ def main():
     name, (tms, nl) = top
     per_launch_ms = tms / max(1, nl)
     nbf, naux, nocc, nnz = ds.nbf, ds.naux, mol.nocc, ds.layout.nnz
-    flops = {
+    pairs = 15  # BF16 digit-pair products per FP64 product (5 digits, s+t <= 4)
+    flops64 = {
         "half_transform": 2.0 * nocc * nnz,
         "fit": 2.0 * naux * naux * nbf * nocc / 2.0,  # lower-triangular L^-1
         "k_gemm": 1.0 * naux * nocc * nbf * (nbf + 1),
+        "split_gemm_ht": 2.0 * nocc * nnz,
+        "split_gemm_k": 1.0 * naux * nocc * nbf * (nbf + 1),
     }
     roof = None
-    if name in flops:
+    if name.startswith("split_gemm"):
+        f = pairs * flops64[name]
+        ach = f / (per_launch_ms * 1e-3) / 1e12
+        roof = {"kernel": "k_split_gemm (" + name + ")", "bound": "tensor", "achieved": ach,
+                "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16, "traffic": None,
+                "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)",
+                "algorithmic_flops_per_launch": f,
+                "flops_definition": "15 BF16 digit-pair products x 2*M*N*K of the unpadded "
+                                    "FP64 product (M*N*K = nocc*nnz(B) for the half transform)",
+                "fp64_equivalent_tflops": flops64[name] / (per_launch_ms * 1e-3) / 1e12,
+                "ms_per_launch": per_launch_ms}
+    elif name in flops64:
         fp64_peak = 1250.0  # GB300 nominal FP64 (GFLOP/s), not in MEASURED_PEAKS.json
-        ach = flops[name] / (per_launch_ms * 1e-3) / 1e12
+        ach = flops64[name] / (per_launch_ms * 1e-3) / 1e12
         roof = {"kernel": name, "bound": "fp64", "achieved": ach, "peak": fp64_peak / 1e3,
                 "unit": "TFLOP/s", "frac": ach / (fp64_peak / 1e3), "traffic": None,
                 "peak_source": "nominal FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)",
-                "algorithmic_flops_per_launch": flops[name], "ms_per_launch": per_launch_ms}
+                "algorithmic_flops_per_launch": flops64[name], "ms_per_launch": per_launch_ms}
     elif name in ("j_rowdot", "j_colsum"):
         byts = nnz * 8.0
         ach = byts / (per_launch_ms * 1e-3) / 1e9
@@ -279,10 +294,41 @@ def main():
                 "frac": ach / hbm, "traffic": None, "peak_source": src,
                 "algorithmic_bytes_per_launch": byts, "ms_per_launch": per_launch_ms}
 
+    # FP64 GPU path beside it: speed and accuracy deltas
+    fp64 = None
+    if args.precision == "split" and not args.no_fp64_compare:
+        Jm, Km = eng.compute_jk(Ph, Cocc, args.kmethod)
+        eng.set_precision("fp64")
+        eng.compute_jk(Ph, Cocc, args.kmethod)
+        nst = max(2, min(args.steps, 5))
+        torch.cuda.synchronize()
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        for _ in range(nst):
+            step()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        ms64 = f0.elapsed_time(f1) / nst
+        Jf, Kf = eng.compute_jk(Ph, Cocc, args.kmethod)
+        eng.set_precision(args.precision)
+        fp64 = {"value": world * 1e3 / ms64, "unit": "builds/s", "ms_per_step": ms64,
+                "steps": nst,
+                "speedup_mixed_over_fp64": ms64 / ms,
+                "max_abs_dK": float(np.abs(Km - Kf).max()),
+                "max_abs_dJ": float(np.abs(Jm - Jf).max()),
+                "dE_Eh": float(np.sum(P * ((Jm - Jf) + (Km - Kf)))),
+                "dE_K_Eh": float(np.sum(P * (Km - Kf))),
+                "dE_definition": "sum P_alpha ((J + K)_mixed - (J + K)_fp64): energy change "
+                                 "of one Fock build at the bench density (E = sum P_alpha "
+                                 "(H + F), F = H + J + K)"}
+
     out = {
         "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 in/out; bf16 digit slices x5 on tcgen05, exact int64 recombination"
+                 if args.precision == "split" else "f64",
         "data": "synthetic molecule (seed-free alkane rule), host-computed integrals",
         "config": workload_config(ds, mol, args.alkane, args.precision, world),
         "e2e": {"value": world * 1e3 / e2e_ms, "unit": "builds/s",
@@ -290,6 +336,7 @@ def main():
                 "d2h_bytes_per_step": int(2 * n * n * 8)},
         "gpu_launches": int(launches),
         "roofline": roof,
+        "fp64_gpu": fp64,
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[1]},
         "clocks": clk.summary(),
         "setup_s": {"integrals_host": round(tset, 2)},

@@ -436,11 +436,6 @@ gbjk_status run_k(gbjk_ctx* ctx, int kmethod, const double* dC, int nocc, double
                                                              ctx->ncols_total, ctx->d_Cg);
     CKL(PH_GATHER);
   }
-  if (ctx->precision == GBJK_SPLIT_BF16) {
-    if ((s = split_run_k(ctx->split, ctx->stream, kmethod, nocc, dK, &ctx->launches, &ctx->err)))
-      return s;
-    return filter(ctx, dK);
-  }
   if ((s = launch_gemm(ctx, ctx->ht_tile0, ctx->ht_ntiles, false, 1.0, PH_HT))) return s;
   const bool mo = kmethod == GBJK_K_DFMO;
   if ((s = launch_gemm(ctx, mo ? ctx->fit_tile0 : ctx->fitV_tile0, ctx->fit_ntiles, false, 1.0,
@@ -628,8 +623,58 @@ static gbjk_status check_ready(gbjk_ctx* ctx) {
 
 static gbjk_status prepare_split(gbjk_ctx* ctx, int nocc) {
   if (ctx->precision != GBJK_SPLIT_BF16) return GBJK_OK;
-  return ctx->split.prepare(ctx->stream, ctx->d_B, ctx->d_Linv, ctx->d_Vinv, ctx->d_Cg, nocc,
-                            ctx->nslices, &ctx->launches, &ctx->dev_bytes, &ctx->err);
+  return ctx->split.prepare(ctx->stream, ctx->d_B, ctx->d_Linv, ctx->d_Cg, ctx->d_Pg,
+                            ctx->pg_off, nocc, &ctx->launches, &ctx->err);
+}
+
+// Mixed-precision J + K.  The density rows of every panel ride along as
+// extra B-operand rows of the split half transform, whose epilogue emits
+// the partials of dt = L^-1 g; J = (L^-1 B)^T dt is one FP64 pass over the
+// prefitted tensor.  Without dJ the density rows are zero.
+static gbjk_status run_jk_split(gbjk_ctx* ctx, const double* dP, const double* dC, int nocc,
+                                double* dJ, double* dK) {
+  const int nbf = ctx->nbf, naux = ctx->naux;
+  gbjk_status s;
+  if (dJ) {
+    PhaseScope ps(ctx, PH_GATHER);
+    k_gather_panel_rows<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, 0, ctx->stream>>>(
+        dP, nbf, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK, ctx->d_pg_off, ctx->d_cmoff,
+        ctx->d_colmap, ctx->d_Pg);
+    CKL(PH_GATHER);
+  } else {
+    CK(cudaMemsetAsync(ctx->d_Pg, 0, (size_t)ctx->pg_total * sizeof(double), ctx->stream));
+  }
+  {
+    PhaseScope ps(ctx, PH_GATHER);
+    const long long total = (long long)ctx->ncols_total * nocc;
+    k_gather_cols<<<cdiv(total, 256), 256, 0, ctx->stream>>>(dC, nocc, ctx->d_colmap,
+                                                             ctx->ncols_total, ctx->d_Cg);
+    CKL(PH_GATHER);
+  }
+  if ((s = ctx->split.run_k(ctx->stream, dK, &ctx->launches, &ctx->err))) return s;
+  if ((s = filter(ctx, dK))) return s;
+  if (!dJ) return GBJK_OK;
+  CK(cudaMemsetAsync(dJ, 0, (size_t)nbf * nbf * sizeof(double), ctx->stream));
+  {
+    PhaseScope ps(ctx, PH_J_REDUCE);
+    k_reduce_rows<<<cdiv(naux, 128), 128, 0, ctx->stream>>>(ctx->split.d_dpart, nbf, naux,
+                                                            ctx->split.d_dt);
+    CKL(PH_J_REDUCE);
+  }
+  {
+    PhaseScope ps(ctx, PH_J_COLSUM);
+    const size_t hbytes = (size_t)naux * sizeof(double);
+    if (hbytes > 48 * 1024 && !ctx->colsum_smem_set) {
+      CK(cudaFuncSetAttribute(k_j_colsum, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)hbytes));
+      ctx->colsum_smem_set = true;
+    }
+    k_j_colsum<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, hbytes, ctx->stream>>>(
+        ctx->split.Bfit, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK,
+        ctx->d_cmoff, ctx->d_colmap, ctx->split.d_dt, nbf, naux, dJ);
+    CKL(PH_J_COLSUM);
+  }
+  return filter(ctx, dJ);
 }
 
 gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, const double* dC,
@@ -644,6 +689,7 @@ gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, co
   if (dK) {
     if ((s = ensure_k_workspace(ctx, nocc))) return s;
     if ((s = prepare_split(ctx, nocc))) return s;
+    if (ctx->precision == GBJK_SPLIT_BF16) return run_jk_split(ctx, dP, dC, nocc, dJ, dK);
   }
   if (dJ && (s = run_j(ctx, dP, dJ))) return s;
   if (dK && (s = run_k(ctx, kmethod, dC, nocc, dK))) return s;

@@ -2,31 +2,32 @@
 // the 5th-generation tensor cores (tcgen05.mma, accumulators in TMEM).
 //
 // Number format.  Row r of an FP64 operand gets an exponent e_r with
-// |x| < 2^e_r for every x of the row.  x is rounded to the 40-bit integer
-// X = rint(|x| 2^(40-e_r)) and written in balanced base-256 digits
-//   X = sum_{j=0..4} d_j 256^j,  d_0..d_3 in [-128, 127],  d_4 in [0, 256],
+// |x| < 2^e_r for every x of the row.  x is rounded to the 39-bit integer
+// X = rint(|x| 2^(39-e_r)) and written in balanced base-256 digits
+//   X = sum_{j=0..4} d_j 256^j,  d_0..d_3 in [-128, 127],  d_4 in [0, 128],
 // which are exact in BF16.  Slice s (s = 0 most significant) holds
 // sign(x) * d_{4-s}.  The extraction uses integer operations only.
 //
-// Product.  sum_k x_A x_B = 2^(eA+eB-80) sum_{s,t} r_{st} 256^(8-s-t),
-// r_{st} = sum_k a_s b_t.  Pairs with s+t <= 4 are kept (15 BF16 MMAs per
-// k-step).  Diagonals d = s+t = 0, 1, 2 are summed exactly: over a chunk of
-// 128 k every partial sum is an integer below 2^24, hence exact in the FP32
-// TMEM accumulator; after each chunk the epilogue warps convert them to
-// integers and add W = r0 256^2 + r1 256 + r2 into an int64 register.
-// Diagonals 3 and 4 accumulate in FP32 over the whole k range (their weight
-// is 2^-24 and 2^-32 of the leading term).  The result,
-//   2^(eA+eB-32) (W + rint(r3/256) + rint(r4/65536)),
-// is assembled into an FP64 bit pattern with integer operations.
+// Product.  sum_k x_A x_B = 2^(eA+eB-78) sum_{s,t} r_{st} 256^(8-s-t),
+// r_{st} = sum_k a_s b_t.  Pairs with s+t <= 4 are kept (15 BF16 digit
+// products per k).  Diagonals d = s+t = 0, 1, 2 are summed exactly: every
+// digit product is at most 2^14 in magnitude, so over a chunk of 256 k every
+// partial sum is an integer below 2^24, hence exact in the FP32 TMEM
+// accumulator; after each chunk the epilogue converts them to integers and
+// adds W = r0 256^2 + r1 256 + r2 into an int64 register.  Diagonals 3 and 4
+// accumulate in FP32 over the whole k range (weights 2^-24 and 2^-32 of the
+// leading term) and are folded in with 16 fractional bits:
+//   value = 2^(eA+eB-46) (W 2^16 + rint(256 r3) + rint(r4)),
+// assembled into an FP64 bit pattern with integer operations.
 //
 // Pipeline (one CTA per SM, persistent over a work list):
 //   warp 0      producer: 1-D bulk copies (cp.async.bulk) of pre-tiled slice
 //               images into a 3-stage shared-memory ring (mbarrier tx count)
 //   warp 1      TMEM allocation and the single MMA-issuing thread
-//   warps 2..9  epilogue: drain exact diagonals per chunk, write results
+//   warps 2..13 epilogue: drain exact diagonals per chunk, write results
 // Per k-tile the MMA thread issues the exact-diagonal pairs first and commits
-// them, then the 9 approximate pairs, so the drain of chunk c overlaps the
-// approximate MMAs.  Every wait is bounded (kSpinNs); on timeout the CTA
+// them, then the 9 approximate pairs (15 pairs as 9 MMAs of N = 96 or 192),
+// so the drain of chunk c overlaps the approximate MMAs.  Every wait is bounded (kSpinNs); on timeout the CTA
 // records an error code, drains its own copies and MMAs and frees TMEM.
 //
 // Shared-memory operand layout: K-major, no swizzle, 8x8 core matrices
@@ -52,10 +53,11 @@ constexpr int kSlices = 5;        // digits per operand
 constexpr int kTileM = 128;       // rows of A per tile (TMEM lanes)
 constexpr int kTileN = 96;        // rows of B per tile (accumulator columns)
 constexpr int kTileK = 32;        // k per pipeline stage
-constexpr int kChunkTiles = 4;    // k-tiles per exact chunk (128 k)
+constexpr int kChunkTiles = 8;    // k-tiles per exact chunk (256 k)
 constexpr int kStages = 3;
 constexpr int kImage = 1024;      // bf16 elements per 32x32 slice image
-constexpr int kEpiWarps = 8;
+constexpr int kEpiWarps = 12;      // 3 per TMEM lane quadrant, 32 columns each
+constexpr int kEpiCols = kTileN / 3;
 constexpr int kThreads = 32 * (2 + kEpiWarps);
 constexpr int kTmemCols = 512;
 constexpr unsigned long long kSpinNs = 2000000000ull;  // 2 s per wait
@@ -76,6 +78,16 @@ struct SplitItem {
   double* out;    // out[r * ldr + c]
   long long ldr;
   int m_valid, n_valid;
+  // optional: atomicMax of the biased FP64 exponent of row r's results into
+  // emax[(emax_row0 + r) / emax_div] (row exponents of the next operand)
+  unsigned int* emax;
+  int emax_row0, emax_div;
+  // optional: columns c0 + col >= ncol1 (c0 = first column of the tile) are
+  // density columns m' = c0 + col - ncol1; the value of row r goes to
+  // out2[emax_row0 + r] when m' == (emax_row0 + r) / emax_div, and is neither
+  // stored in `out` nor counted in emax
+  double* out2;
+  int c0, ncol1;
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -108,16 +120,20 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait; on timeout records `code` in *err and returns false.
+// Bounded wait; on timeout records `code` in *err and returns false.  The
+// error flag and the timer are read every 1024 polls only, so a completed
+// phase is seen within one try_wait.
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer();
-  while (true) {
+  for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if (*(volatile int*)err != 0) return false;
-    if (globaltimer() - t0 > kSpinNs) {
-      atomicCAS(err, 0, code);
-      return false;
+    if ((i & 1023) == 0) {
+      if (*(volatile int*)err != 0) return false;
+      if (globaltimer() - t0 > kSpinNs) {
+        atomicCAS(err, 0, code);
+        return false;
+      }
     }
   }
 }
@@ -176,30 +192,65 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// |v| < 2^53 times 2^e2 as an FP64 bit pattern, integer operations only.
+// rint(v * 2^k) for an FP32 value v, |v * 2^k| < 2^62, with integer
+// operations only (no 64-bit conversion instruction).
+__device__ __forceinline__ long long f32_scaled_rint(float v, int k) {
+  const unsigned int u = __float_as_uint(v);
+  const int E = (int)((u >> 23) & 0xFF);
+  if (E == 0) return 0;  // zero or subnormal (|v| < 2^-126)
+  const long long m = (long long)((u & 0x7FFFFF) | 0x800000);
+  const int sh = E - 150 + k;  // v * 2^k = m * 2^sh
+  long long r;
+  if (sh >= 0)
+    r = m << sh;
+  else if (sh > -25)
+    r = (m + (1ll << (-sh - 1))) >> (-sh);
+  else
+    r = 0;
+  return (u >> 31) ? -r : r;
+}
+
+// v * 2^e2 rounded to nearest FP64, as a bit pattern built with integer
+// operations only (|v| < 2^63).
 __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e2) {
   if (v == 0) return 0.0;
   const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
   const unsigned long long m = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
-  const int msb = 63 - __clzll((long long)m);
+  int msb = 63 - __clzll((long long)m);
+  unsigned long long frac;
+  if (msb <= 52) {
+    frac = m << (52 - msb);
+  } else {
+    const int sh = msb - 52;
+    unsigned long long mr = m + (1ull << (sh - 1));  // round half up
+    if (msb < 63 && (mr >> (msb + 1))) {             // carry into a new top bit
+      ++msb;
+      frac = mr >> (sh + 1);
+    } else {
+      frac = mr >> sh;
+    }
+  }
+  frac &= (1ull << 52) - 1;
   const long long ex = (long long)msb + e2 + 1023;
   if (ex <= 0) return 0.0;
   if (ex >= 2047) return __longlong_as_double((long long)(sgn | (0x7FFull << 52)));
-  const unsigned long long frac =
-      (msb <= 52 ? (m << (52 - msb)) : (m >> (msb - 52))) & ((1ull << 52) - 1);
   return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | frac));
 }
 
 // ------------------------------------------------------------ split kernels
-// A split job describes one FP64 operand: element (r, c) = src[r*rs + c*cs]
-// for r < nrows, c < ncols (zero elsewhere up to nrb*32 rows, nkt*32 cols);
-// row exponents go to e[r], slice images to dst as [kt][s][rb][1024].
+// A split job fills rows [row0, row0 + nrows) of one digit operand:
+// element (r, c) = src[(r - row0)*rs + c*cs] for c < ncols, zero for
+// ncols <= c < nkt*32.  Row exponents are e[r] (e_biased != 0: e holds the
+// maximum biased FP64 exponent of the row, 0 for an all-zero row).  Slice
+// images go to dst as [kt][s][rb][1024]; rows outside every job stay as
+// allocated (zero).
 struct SplitJob {
   const double* src;
   long long rs, cs;
-  int nrows;
+  int row0, nrows;
   long long ncols;
   int* e;
+  int e_biased;
   int nrb, nkt;
   uint16_t* dst;
 };
@@ -208,53 +259,61 @@ struct SplitJob {
 // an all-zero row.  grid (rows/8, njobs), one warp per row.
 __global__ void k_row_maxexp(const SplitJob* __restrict__ jobs) {
   const SplitJob jb = jobs[blockIdx.y];
-  const long long row = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long i = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
-  if (row >= jb.nrb * 32) return;
+  if (i >= jb.nrows) return;
   unsigned int mx = 0;
-  if (row < jb.nrows) {
-    const double* p = jb.src + row * jb.rs;
-    for (long long c = lane; c < jb.ncols; c += 32) {
-      const unsigned long long u = (unsigned long long)__double_as_longlong(p[c * jb.cs]);
-      mx = max(mx, (unsigned int)((u >> 52) & 0x7FF));
-    }
+  const double* p = jb.src + i * jb.rs;
+  for (long long c = lane; c < jb.ncols; c += 32) {
+    const unsigned long long u = (unsigned long long)__double_as_longlong(p[c * jb.cs]);
+    mx = max(mx, (unsigned int)((u >> 52) & 0x7FF));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if (lane == 0) jb.e[row] = mx == 0 ? -2000 : (int)mx - 1022;
+  if (lane == 0) jb.e[jb.row0 + i] = mx == 0 ? -2000 : (int)mx - 1022;
+}
+
+// Biased FP64 exponent maxima (0 = all zero) -> row exponents in place.
+__global__ void k_exp_unbias(int* __restrict__ e, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) e[i] = e[i] == 0 ? -2000 : e[i] - 1022;
 }
 
 __device__ __forceinline__ uint16_t small_int_to_bf16(int d) {
   // d in [-2^22, 2^22): exact float via the 1.5*2^23 magic, then BF16 bits
-  // (exact: |d| <= 256 needs at most 9 significant bits)
+  // (exact: |d| <= 128 needs at most 8 significant bits)
   const float f = __int_as_float(0x4B400000 + d) - 12582912.0f;
   return (uint16_t)(__float_as_uint(f) >> 16);
 }
 
-// Slice images; grid (ceil(max_threads/256), njobs), one thread per
-// (row, 8-column group).
+// Slice images.  One warp per (8-row group, k-tile): lane (rr, kc) =
+// (lane & 7, lane >> 3) handles row 8g + rr, columns 32kt + 8kc .. +7, so
+// each warp writes 512 contiguous bytes per slice.  grid (warps/8, njobs).
 __global__ void k_split_tiles(const SplitJob* __restrict__ jobs) {
   const SplitJob jb = jobs[blockIdx.y];
-  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const long long nrows_pad = (long long)jb.nrb * 32;
-  const long long total = nrows_pad * jb.nkt * 4;
-  if (idx >= total) return;
-  const int r = (int)(idx % nrows_pad);
-  const long long cg = idx / nrows_pad;  // 8-column group
-  const int kt = (int)(cg >> 2), kc = (int)(cg & 3);
+  const long long wid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int g0 = jb.row0 >> 3, g1 = (jb.row0 + jb.nrows + 7) >> 3;
+  const int ng = g1 - g0;
+  if (wid >= (long long)ng * jb.nkt) return;
+  const int g = g0 + (int)(wid % ng), kt = (int)(wid / ng);
+  const int rr = lane & 7, kc = lane >> 3;
+  const int r = 8 * g + rr;
+  if (r < jb.row0 || r >= jb.row0 + jb.nrows) return;
+  int er = jb.e[r];
+  if (jb.e_biased) er = er == 0 ? -2000 : er - 1022;
+  const double* src = jb.src + (long long)(r - jb.row0) * jb.rs;
   uint16_t out[kSlices][8];
-  const int er = r < jb.nrows ? jb.e[r] : -2000;
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const long long c = cg * 8 + j;
-    double x = 0.0;
-    if (r < jb.nrows && c < jb.ncols) x = jb.src[(long long)r * jb.rs + c * jb.cs];
+    const long long c = (long long)kt * 32 + kc * 8 + j;
+    const double x = c < jb.ncols ? src[c * jb.cs] : 0.0;
     const unsigned long long u = (unsigned long long)__double_as_longlong(x);
     const int E = (int)((u >> 52) & 0x7FF);
     unsigned long long X = 0;
     if (E != 0 && er > -2000) {
       const unsigned long long m = (u & ((1ull << 52) - 1)) | (1ull << 52);
-      const int sh = 1035 + er - E;  // X = rint(m / 2^sh); sh >= 13 since |x| < 2^er
+      const int sh = 1036 + er - E;  // X = rint(m / 2^sh); sh >= 14 since |x| < 2^er
       if (sh < 64) X = (m + (1ull << (sh - 1))) >> sh;
     }
     const bool neg = (u >> 63) != 0;
@@ -269,8 +328,8 @@ __global__ void k_split_tiles(const SplitJob* __restrict__ jobs) {
       out[s][j] = small_int_to_bf16(neg ? -d : d);
     }
   }
-  const int rb = r >> 5, rr = r & 31;
-  const long long off_in = (long long)(rr >> 3) * 256 + kc * 64 + (rr & 7) * 8;
+  const int rb = r >> 5;
+  const long long off_in = (long long)((r & 31) >> 3) * 256 + kc * 64 + rr * 8;
 #pragma unroll
   for (int s = 0; s < kSlices; ++s) {
     uint16_t* p = jb.dst + (((long long)kt * kSlices + s) * jb.nrb + rb) * kImage + off_in;
@@ -284,11 +343,8 @@ __global__ void k_split_tiles(const SplitJob* __restrict__ jobs) {
 }
 
 // ------------------------------------------------------------ the GEMM
-// Pairs (s, t) in issue order: exact diagonals first (d = 0, 1, 2), then
-// d = 3, 4.  Accumulator of diagonal d at TMEM column d * kTileN.
-__constant__ unsigned char c_pair_s[15] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4};
-__constant__ unsigned char c_pair_t[15] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 4, 3, 2, 1, 0};
-constexpr int kExactPairs = 6;
+// Pairs (s, t) are issued exact diagonals first (d = 0, 1, 2), then d = 3, 4;
+// the accumulator of diagonal d sits at TMEM column d * kTileN.
 
 __global__ void __launch_bounds__(kThreads, 1)
     k_split_gemm(const SplitItem* __restrict__ items, int nitems, int* __restrict__ err) {
@@ -368,6 +424,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // ---------------- MMA issuer
     if (lane == 0) {
       const uint32_t idesc = instr_desc(kTileM, kTileN);
+      const uint32_t idesc2 = instr_desc(kTileM, 2 * kTileN);
       int stage = 0;
       uint32_t phase = 0;
       uint32_t ex_phase = 0, fin_phase = 0;
@@ -388,21 +445,32 @@ __global__ void __launch_bounds__(kThreads, 1)
           ok = mbar_wait(&full_bar[stage], phase, err, 5);
           if (!ok) break;
           tc_fence_after();
-          const uint32_t a0 = smem_u32(sA + stage * kBytesA);
-          const uint32_t b0 = smem_u32(sB + stage * kBytesB);
-          for (int p = 0; p < 15; ++p) {
-            if (p == kExactPairs && chunk_end) mma_commit(&exact_full);
-            const int s = c_pair_s[p], t = c_pair_t[p];
-            const int d = s + t;
-            const uint32_t dcol = tmem + (uint32_t)(d * kTileN);
+          const uint64_t adesc = smem_desc(smem_u32(sA + stage * kBytesA));
+          const uint64_t bdesc = smem_desc(smem_u32(sB + stage * kBytesB));
+          // descriptor start addresses advance in 16-byte units
+          constexpr uint32_t kSliceA = kTileM * kTileK * 2 / 16, kSliceB = kTileN * kTileK * 2 / 16;
+          // The 15 slice pairs (s, t), s + t <= 4, as 9 MMAs: B slices t0 and
+          // t0+1 are adjacent in shared memory and diagonals d and d+1 have
+          // adjacent accumulators, so one N = 192 MMA updates both.  Entries:
+          // {s, t0, number of B slices, reset class}; reset class 1 = first
+          // write of exact diagonals (reset at a chunk start), 2 = first write
+          // of d = 3, 4 (reset at the item's first k-tile).  The first four
+          // MMAs cover exactly the diagonals 0..2.
+#pragma unroll
+          for (int q = 0; q < 9; ++q) {
+            constexpr unsigned char qs[9] = {0, 0, 1, 2, 0, 1, 2, 3, 4};
+            constexpr unsigned char qt[9] = {0, 2, 0, 0, 3, 2, 1, 0, 0};
+            constexpr unsigned char qn[9] = {2, 1, 2, 1, 2, 2, 2, 2, 1};
+            constexpr unsigned char qr[9] = {1, 1, 0, 0, 2, 0, 0, 0, 0};
+            if (q == 4 && chunk_end) mma_commit(&exact_full);
+            const uint32_t dcol = tmem + (uint32_t)((qs[q] + qt[q]) * kTileN);
+            const uint32_t id = qn[q] == 2 ? idesc2 : idesc;
+            const bool reset = qr[q] == 1 ? chunk_start : (qr[q] == 2 ? k == 0 : false);
+#pragma unroll
             for (int j = 0; j < 2; ++j) {
-              const uint64_t ad = smem_desc(a0 + s * (kTileM * kTileK * 2) + j * 256);
-              const uint64_t bd = smem_desc(b0 + t * (kTileN * kTileK * 2) + j * 256);
-              // exact diagonals restart every chunk, the others every item;
-              // the first pair of each diagonal in a tile's first k16 resets
-              const bool first_k = (d < 3 ? chunk_start : k == 0) && j == 0;
-              const bool first_pair = (p == 0 || p == 1 || p == 3 || p == 6 || p == 10);
-              mma_bf16(dcol, ad, bd, idesc, (first_k && first_pair) ? 0u : 1u);
+              const uint64_t ad = adesc + (uint64_t)(qs[q] * kSliceA + j * 16);
+              const uint64_t bd = bdesc + (uint64_t)(qt[q] * kSliceB + j * 16);
+              mma_bf16(dcol, ad, bd, id, (reset && j == 0) ? 0u : 1u);
             }
           }
           mma_commit(&empty_bar[stage]);
@@ -415,36 +483,41 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    // ---------------- epilogue (warps 2..9)
+    // ---------------- epilogue (warps 2..13)
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
-    const int half = (warp - 2) >> 2;       // column half: 0 or 1
+    const int half = (warp - 2) >> 2;       // column third: 0, 1 or 2
     const int row = q * 32 + lane;          // tile-local row
     const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
     uint32_t ex_phase = 0, fin_phase = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
       const SplitItem w = items[it];
-      long long V[kTileN / 2];
+      long long V[kEpiCols];
 #pragma unroll
-      for (int c = 0; c < kTileN / 2; ++c) V[c] = 0;
+      for (int c = 0; c < kEpiCols; ++c) V[c] = 0;
       const int nchunks = (w.nkt + kChunkTiles - 1) / kChunkTiles;
       for (int ch = 0; ch < nchunks && ok; ++ch) {
         ok = mbar_wait(&exact_full, ex_phase, err, 6);
         ex_phase ^= 1;
         if (!ok) break;
         tc_fence_after();
+        // d0 is at most 2^22 in magnitude: converted with the 1.5*2^23 magic
+        // (one FADD); d1, d2 (below 2^24) with a rounding conversion
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
+        for (int g = 0; g < kEpiCols / 16; ++g) {
+          uint32_t v0[16], v1[16], v2[16];
+          const uint32_t col = (uint32_t)(half * kEpiCols + g * 16);
+          tmem_ld16(tmem + lane_addr + col, v0);
+          tmem_ld16(tmem + lane_addr + (uint32_t)kTileN + col, v1);
+          tmem_ld16(tmem + lane_addr + (uint32_t)(2 * kTileN) + col, v2);
+          tmem_wait_ld();
 #pragma unroll
-          for (int g = 0; g < kTileN / 2 / 16; ++g) {
-            uint32_t v[16];
-            tmem_ld16(tmem + lane_addr + (uint32_t)(d * kTileN + half * (kTileN / 2) + g * 16), v);
-            tmem_wait_ld();
-#pragma unroll
-            for (int c = 0; c < 16; ++c) {
-              const long long r = (long long)__float2int_rn(__uint_as_float(v[c]));
-              V[g * 16 + c] += r << (8 * (2 - d));
-            }
+          for (int c = 0; c < 16; ++c) {
+            const int r0 = __float_as_int(__uint_as_float(v0[c]) + 12582912.0f) - 0x4B400000;
+            const int r1 = __float2int_rn(__uint_as_float(v1[c]));
+            const int r2 = __float2int_rn(__uint_as_float(v2[c]));
+            const int t01 = (r0 << 8) + r1;  // < 2^31
+            V[g * 16 + c] += ((long long)t01 << 8) + r2;
           }
         }
         tc_fence_before();
@@ -456,32 +529,77 @@ __global__ void __launch_bounds__(kThreads, 1)
       fin_phase ^= 1;
       if (!ok) break;
       tc_fence_after();
-      const bool rvalid = row < w.m_valid;
-      const int er = rvalid ? w.ea[row] : 0;
+      // fold the approximate diagonals in with 16 fractional bits:
+      //   V = W 2^16 + rint(256 r3) + rint(r4),  value = V 2^(eA+eB-46)
 #pragma unroll
-      for (int g = 0; g < kTileN / 2 / 16; ++g) {
+      for (int g = 0; g < kEpiCols / 16; ++g) {
         uint32_t v3[16], v4[16];
-        tmem_ld16(tmem + lane_addr + (uint32_t)(3 * kTileN + half * (kTileN / 2) + g * 16), v3);
-        tmem_ld16(tmem + lane_addr + (uint32_t)(4 * kTileN + half * (kTileN / 2) + g * 16), v4);
+        tmem_ld16(tmem + lane_addr + (uint32_t)(3 * kTileN + half * kEpiCols + g * 16), v3);
+        tmem_ld16(tmem + lane_addr + (uint32_t)(4 * kTileN + half * kEpiCols + g * 16), v4);
         tmem_wait_ld();
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          const int col = half * (kTileN / 2) + g * 16 + c;
-          const long long r3 =
-              (long long)__float2ll_rn(__uint_as_float(v3[c]) * (1.0f / 256.0f));
-          const long long r4 =
-              (long long)__float2ll_rn(__uint_as_float(v4[c]) * (1.0f / 65536.0f));
-          const long long vf = V[g * 16 + c] + r3 + r4;
-          if (rvalid && col < w.n_valid) {
-            const int ec = w.eb[col];
-            const double x = (er <= -2000 || ec <= -2000) ? 0.0 : i64_scaled_to_f64(vf, er + ec - 32);
-            w.out[(long long)row * w.ldr + col] = x;
-          }
+          const long long r3 = f32_scaled_rint(__uint_as_float(v3[c]), 8);
+          const long long r4 = f32_scaled_rint(__uint_as_float(v4[c]), 0);
+          V[g * 16 + c] = (V[g * 16 + c] << 16) + r3 + r4;
         }
       }
+      // the accumulators are free for the next item before the stores
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&final_empty);
+      const bool rvalid = row < w.m_valid;
+      unsigned int emax_row = 0;
+      if (rvalid) {
+        const int er = w.ea[row];
+        double* orow = w.out + (long long)row * w.ldr + half * kEpiCols;
+        const int cbase = half * kEpiCols;
+        const bool vec = ((uintptr_t)orow & 15) == 0;
+        const int nstore = min(w.n_valid, w.ncol1 - w.c0);  // columns kept in `out`
+        // density column of this row's AO function (tile-local), or -1
+        int dcol = -1;
+        if (w.out2) {
+          const int cand = w.ncol1 + (w.emax_row0 + row) / w.emax_div - w.c0;
+          if (cand >= 0 && cand < w.n_valid) dcol = cand;
+        }
+#pragma unroll
+        for (int c = 0; c < kEpiCols; c += 2) {
+          const int col = cbase + c;
+          const bool s0 = col < nstore, s1 = col + 1 < nstore;
+          const bool d0 = col == dcol, d1 = col + 1 == dcol;
+          if (!(s0 || s1 || d0 || d1)) continue;
+          const int ec0 = (s0 || d0) ? w.eb[col] : -2000;
+          const int ec1 = (s1 || d1) ? w.eb[col + 1] : -2000;
+          const double x0 =
+              (er <= -2000 || ec0 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c], er + ec0 - 46);
+          const double x1 =
+              (er <= -2000 || ec1 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c + 1], er + ec1 - 46);
+          if (d0) w.out2[w.emax_row0 + row] = x0;
+          if (d1) w.out2[w.emax_row0 + row] = x1;
+          if (s0) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x0) >> 52) & 0x7FF));
+          if (s1) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x1) >> 52) & 0x7FF));
+          if (vec && s0 && s1) {
+            *reinterpret_cast<double2*>(orow + c) = make_double2(x0, x1);
+          } else {
+            if (s0) orow[c] = x0;
+            if (s1) orow[c + 1] = x1;
+          }
+        }
+      }
+      if (w.emax) {
+        // one atomic per warp when all its rows map to the same target row
+        const int target = rvalid ? (w.emax_row0 + row) / w.emax_div : -1;
+        const int t0 = __shfl_sync(0xffffffffu, target, 0);
+        const bool same = __all_sync(0xffffffffu, target == t0);
+        if (same) {
+          unsigned int m = emax_row;
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+          if (lane == 0 && t0 >= 0 && m) atomicMax(w.emax + t0, m);
+        } else if (target >= 0 && emax_row) {
+          atomicMax(w.emax + target, emax_row);
+        }
+      }
     }
   }
   // teardown: everyone joins, then warp 1 frees TMEM once all MMAs are done

@@ -28,7 +28,8 @@ struct SplitState {
   std::vector<long long> panel_off;
   bool b_ready = false;
   int nocc = -1;
-  // A operands (static)
+  // A operands (static) and the prefitted tensor L^-1 B (FP64)
+  double* Bfit = nullptr;
   uint16_t* d_Aslices = nullptr;
   std::vector<long long> a_off, eA_off;
   std::vector<int> a_nrb, nkt;
@@ -40,13 +41,16 @@ struct SplitState {
   int* d_eC = nullptr;
   double* d_H = nullptr;
   uint16_t* d_Hslices = nullptr;
-  int h_nrb = 0, h_nkt = 0;
+  int h_nrb = 0, h_nkt = 0, hld = 0;
   int* d_eH = nullptr;
   double* d_Kpart = nullptr;
+  double* d_dpart = nullptr;  // J partials [mu][Y] from the density columns
+  double* d_dt = nullptr;     // L^-1 g
   int ksplit = 1;
+  int maxb = 0;
   SplitItem* d_items = nullptr;
   int ht_nitems = 0, k_nitems = 0;
-  SplitJob* d_jobs = nullptr;  // [0..nblk): C jobs, [nblk]: H job
+  SplitJob* d_jobs = nullptr;  // [0,nblk): C rows, [nblk,2nblk): P rows, [2nblk]: H
   int c_maxthreads = 0, c_maxrows = 0;
   long long h_threads = 0;
   int* d_err = nullptr;
@@ -92,12 +96,15 @@ struct SplitState {
     free_(&d_Hslices);
     free_(&d_eH);
     free_(&d_Kpart);
+    free_(&d_dpart);
+    free_(&d_dt);
     free_(&d_items);
     free_(&d_jobs);
     nocc = -1;
   }
   void release() {
     release_build();
+    free_(&Bfit);
     free_(&d_Aslices);
     free_(&d_eA);
     free_(&d_err);
@@ -256,7 +263,9 @@ struct SplitState {
       atot += (long long)a_nrb[I] * nkt[I] * kSlices * kImage;
       etot += (long long)a_nrb[I] * 32;
     }
-    if (alloc(&d_Aslices, (size_t)atot) != cudaSuccess || alloc(&d_eA, (size_t)etot) != cudaSuccess) {
+    if (alloc(&d_Aslices, (size_t)atot) != cudaSuccess || alloc(&d_eA, (size_t)etot) != cudaSuccess ||
+        cudaMemsetAsync(d_Aslices, 0, (size_t)atot * 2, st) != cudaSuccess ||
+        cudaMemsetAsync(d_eA, 0, (size_t)etot * 4, st) != cudaSuccess) {
       free_(&dg);
       free_(&dt);
       free_(&d_Bfit);
@@ -271,14 +280,16 @@ struct SplitState {
       j.src = d_Bfit + panel_off[I];
       j.rs = panelK[I];
       j.cs = 1;
+      j.row0 = 0;
       j.nrows = bsize[I] * naux;
       j.ncols = panelK[I];
       j.e = d_eA + eA_off[I];
+      j.e_biased = 0;
       j.nrb = a_nrb[I];
       j.nkt = nkt[I];
       j.dst = d_Aslices + a_off[I];
-      maxrows = std::max(maxrows, j.nrb * 32);
-      maxthr = std::max(maxthr, (long long)j.nrb * 32 * j.nkt * 4);
+      maxrows = std::max(maxrows, j.nrows);
+      maxthr = std::max(maxthr, (long long)(j.nrows / 8 + 2) * j.nkt * 32);
     }
     SplitJob* dj = nullptr;
     if (alloc(&dj, jobs.size()) != cudaSuccess) {
@@ -296,8 +307,7 @@ struct SplitState {
     cudaFree(dj);
     cudaFree(dg);
     cudaFree(dt);
-    cudaFree(d_Bfit);
-    bytes -= (size_t)nnz * sizeof(double);
+    Bfit = d_Bfit;  // kept: the mixed-mode J contracts it in FP64
     if (e != cudaSuccess) {
       *err = std::string("split path preparation: ") + cudaGetErrorString(e);
       return GBJK_CUDA_ERROR;
@@ -309,7 +319,10 @@ struct SplitState {
   // --- per nocc: buffers and work lists ------------------------------------
   gbjk_status prepare_nocc(cudaStream_t st, int nocc_, std::string* err) {
     release_build();
-    const int ntn = cdiv_(nocc_, kTileN);
+    maxb = 0;
+    for (int I = 0; I < nblk; ++I) maxb = std::max(maxb, bsize[I]);
+    // B operand rows of panel I: nocc orbitals, then b_I density rows
+    const int ntn = cdiv_(nocc_ + maxb, kTileN);
     c_nrb = ntn * (kTileN / 32);
     c_off.assign(nblk, 0);
     long long ctot = 0;
@@ -317,7 +330,8 @@ struct SplitState {
       c_off[I] = ctot;
       ctot += (long long)c_nrb * nkt[I] * kSlices * kImage;
     }
-    const long long hk = (long long)naux * nocc_;
+    hld = nocc_ + (nocc_ & 1);  // even row stride: 16-byte aligned pairs
+    const long long hk = (long long)naux * hld;
     h_nkt = cdiv_(hk, kTileK);
     h_nrb = std::max(cdiv_(nbf, kTileM) * (kTileM / 32), cdiv_(nbf, kTileN) * (kTileN / 32));
     const int kt_per = 256;  // at most 8192 k per exchange item
@@ -327,7 +341,14 @@ struct SplitState {
         alloc(&d_H, (size_t)nbf * hk) != cudaSuccess ||
         alloc(&d_Hslices, (size_t)h_nrb * h_nkt * kSlices * kImage) != cudaSuccess ||
         alloc(&d_eH, (size_t)h_nrb * 32) != cudaSuccess ||
-        alloc(&d_Kpart, (size_t)ksplit * nbf * nbf) != cudaSuccess) {
+        alloc(&d_Kpart, (size_t)ksplit * nbf * nbf) != cudaSuccess ||
+        alloc(&d_dpart, (size_t)nbf * naux) != cudaSuccess ||
+        alloc(&d_dt, (size_t)naux) != cudaSuccess ||
+        cudaMemsetAsync(d_Cslices, 0, (size_t)ctot * 2, st) != cudaSuccess ||
+        cudaMemsetAsync(d_eC, 0, (size_t)nblk * c_nrb * 32 * 4, st) != cudaSuccess ||
+        cudaMemsetAsync(d_H, 0, (size_t)nbf * hk * 8, st) != cudaSuccess ||
+        cudaMemsetAsync(d_Hslices, 0, (size_t)h_nrb * h_nkt * kSlices * kImage * 2, st) !=
+            cudaSuccess) {
       release_build();
       *err = "split path: out of memory for the per-build buffers";
       return GBJK_OOM;
@@ -336,8 +357,9 @@ struct SplitState {
     // half transform: Hfit rows (m, Y) of panel I, columns i
     for (int I = 0; I < nblk; ++I) {
       const long long rows = (long long)bsize[I] * naux;
+      const int ncolI = nocc_ + bsize[I];
       for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
-        for (int nt = 0; nt < ntn; ++nt) {
+        for (int nt = 0; nt < cdiv_(ncolI, kTileN); ++nt) {
           SplitItem w;
           w.a = d_Aslices + a_off[I];
           w.a_nrb = a_nrb[I];
@@ -349,11 +371,19 @@ struct SplitState {
           w.nkt = nkt[I];
           w.ea = d_eA + eA_off[I] + (long long)mt * kTileM;
           w.eb = d_eC + (long long)I * c_nrb * 32 + (long long)nt * kTileN;
-          w.out = d_H + ((long long)boff[I] * naux + (long long)mt * kTileM) * nocc_ +
+          w.out = d_H + ((long long)boff[I] * naux + (long long)mt * kTileM) * hld +
                   (long long)nt * kTileN;
-          w.ldr = nocc_;
+          w.ldr = hld;
           w.m_valid = (int)std::min<long long>(kTileM, rows - (long long)mt * kTileM);
-          w.n_valid = std::min(kTileN, nocc_ - nt * kTileN);
+          w.n_valid = std::min(kTileN, ncolI - nt * kTileN);
+          // row (m, Y) of panel I belongs to H row mu = boff[I] + m
+          w.emax = (unsigned int*)d_eH + boff[I];
+          w.emax_row0 = mt * kTileM;
+          w.emax_div = naux;
+          // density column m' = col - nocc: g-partial of row (m, Y) if m' == m
+          w.out2 = d_dpart + (long long)boff[I] * naux;
+          w.c0 = nt * kTileN;
+          w.ncol1 = nocc_;
           items.push_back(w);
         }
     }
@@ -381,37 +411,59 @@ struct SplitState {
           w.ldr = nbf;
           w.m_valid = std::min(kTileM, nbf - mt * kTileM);
           w.n_valid = std::min(kTileN, nbf - nt * kTileN);
+          w.emax = nullptr;
+          w.emax_row0 = 0;
+          w.emax_div = 1;
+          w.out2 = nullptr;
+          w.c0 = 0;
+          w.ncol1 = 1 << 30;
           items.push_back(w);
         }
     }
     k_nitems = (int)items.size() - ht_nitems;
-    std::vector<SplitJob> jobs(nblk + 1);
+    std::vector<SplitJob> jobs(2 * nblk + 1);
     c_maxthreads = 0;
-    c_maxrows = c_nrb * 32;
+    c_maxrows = std::max(nocc_, maxb);
     for (int I = 0; I < nblk; ++I) {
+      SplitJob& pj = jobs[nblk + I];  // density rows: Pg panel rows
+      pj.src = nullptr;               // set per build
+      pj.rs = panelK[I];
+      pj.cs = 1;
+      pj.row0 = nocc_;
+      pj.nrows = bsize[I];
+      pj.ncols = panelK[I];
+      pj.e = d_eC + (long long)I * c_nrb * 32;
+      pj.e_biased = 0;
+      pj.nrb = c_nrb;
+      pj.nkt = nkt[I];
+      pj.dst = d_Cslices + c_off[I];
       SplitJob& j = jobs[I];
       j.src = nullptr;  // set per build (Cg pointer owned by the context)
       j.rs = 1;
       j.cs = nocc_;
+      j.row0 = 0;
       j.nrows = nocc_;
       j.ncols = panelK[I];
       j.e = d_eC + (long long)I * c_nrb * 32;
+      j.e_biased = 0;
       j.nrb = c_nrb;
       j.nkt = nkt[I];
       j.dst = d_Cslices + c_off[I];
-      c_maxthreads = std::max(c_maxthreads, c_nrb * 32 * nkt[I] * 4);
+      c_maxthreads = std::max(c_maxthreads, ((nocc_ + maxb) / 8 + 2) * nkt[I] * 32);
     }
-    SplitJob& hj = jobs[nblk];
+    SplitJob& hj = jobs[2 * nblk];
     hj.src = d_H;
     hj.rs = hk;
     hj.cs = 1;
+    hj.row0 = 0;
     hj.nrows = nbf;
     hj.ncols = hk;
-    hj.e = d_eH;
+    hj.e = d_eH;  // from the half-transform epilogue, unbiased before use
+    hj.e_biased = 0;
     hj.nrb = h_nrb;
     hj.nkt = h_nkt;
     hj.dst = d_Hslices;
-    h_threads = (long long)h_nrb * 32 * h_nkt * 4;
+    h_threads = (long long)(nbf / 8 + 2) * h_nkt * 32;
     if (alloc(&d_items, items.size()) != cudaSuccess || alloc(&d_jobs, jobs.size()) != cudaSuccess) {
       release_build();
       *err = "split path: out of memory for the work lists";
@@ -425,15 +477,20 @@ struct SplitState {
   }
   std::vector<SplitJob> host_jobs;
   const double* jobs_cg = nullptr;
+  const double* jobs_pg = nullptr;
 
   gbjk_status prepare(cudaStream_t st, const double* d_B, const double* d_Linv,
-                      const double* /*d_Vinv*/, const double* d_Cg_, int nocc_, int /*nslices*/,
-                      int64_t* launches, size_t* /*dev_bytes*/, std::string* err) {
+                      const double* d_Cg_, const double* d_Pg, const std::vector<long long>& pg_off,
+                      int nocc_, int64_t* launches, std::string* err) {
     gbjk_status s;
     if (!b_ready && (s = prepare_b(st, d_B, d_Linv, launches, err))) return s;
     if (nocc != nocc_ && (s = prepare_nocc(st, nocc_, err))) return s;
-    if (jobs_cg != d_Cg_) {
-      for (int I = 0; I < nblk; ++I) host_jobs[I].src = d_Cg_ + (long long)cmoff[I] * nocc_;
+    if (jobs_cg != d_Cg_ || jobs_pg != d_Pg) {
+      for (int I = 0; I < nblk; ++I) {
+        host_jobs[I].src = d_Cg_ + (long long)cmoff[I] * nocc_;
+        host_jobs[nblk + I].src = d_Pg + pg_off[I];
+      }
+      jobs_pg = d_Pg;
       if (cudaMemcpy(d_jobs, host_jobs.data(), host_jobs.size() * sizeof(SplitJob),
                      cudaMemcpyHostToDevice) != cudaSuccess) {
         *err = "split path: job upload failed";
@@ -449,18 +506,23 @@ struct SplitState {
     gbjk_status s;
     {
       Scope sc(this, 2, st);
-      k_row_maxexp<<<dim3(cdiv_((long long)c_maxrows * 32, 256), nblk), 256, 0, st>>>(d_jobs);
-      k_split_tiles<<<dim3(cdiv_(c_maxthreads, 256), nblk), 256, 0, st>>>(d_jobs);
+      k_row_maxexp<<<dim3(cdiv_((long long)c_maxrows * 32, 256), 2 * nblk), 256, 0, st>>>(d_jobs);
+      k_split_tiles<<<dim3(cdiv_((long long)c_maxthreads, 256), 2 * nblk), 256, 0, st>>>(d_jobs);
       *launches += 2;
     }
     {
       Scope sc(this, 0, st);
+      // H row exponents are atomically maximised by the half-transform epilogue
+      if (cudaMemsetAsync(d_eH, 0, (size_t)h_nrb * 32 * sizeof(int), st) != cudaSuccess) {
+        *err = "split path: memset failed";
+        return GBJK_CUDA_ERROR;
+      }
       if ((s = launch_gemm(st, d_items, ht_nitems, launches, err))) return s;
     }
     {
       Scope sc(this, 2, st);
-      k_row_maxexp<<<dim3(cdiv_((long long)h_nrb * 32 * 32, 256), 1), 256, 0, st>>>(d_jobs + nblk);
-      k_split_tiles<<<dim3(cdiv_(h_threads, 256), 1), 256, 0, st>>>(d_jobs + nblk);
+      k_exp_unbias<<<cdiv_((long long)h_nrb * 32, 256), 256, 0, st>>>(d_eH, h_nrb * 32);
+      k_split_tiles<<<dim3(cdiv_(h_threads, 256), 1), 256, 0, st>>>(d_jobs + 2 * nblk);
       *launches += 2;
     }
     {
@@ -485,10 +547,5 @@ struct SplitState {
     return h;
   }
 };
-
-inline gbjk_status split_run_k(SplitState& S, cudaStream_t st, int /*kmethod*/, int /*nocc*/,
-                               double* dK, int64_t* launches, std::string* err) {
-  return S.run_k(st, dK, launches, err);
-}
 
 }  // namespace gbjk

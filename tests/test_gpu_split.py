@@ -1,7 +1,8 @@
 """Split-precision (BF16 digit slices on tcgen05 tensor cores) K path against
 the FP64 oracle.  Tolerances are the configs' bars: max|dK| <= 1e-9 and, for
-SCF energies, |dE| <= 1e-8 Eh against the FP64 path.  J stays FP64 in the
-mixed mode and must be bit-identical to the plain path."""
+SCF energies, |dE| <= 1e-8 Eh against the FP64 path.  In the mixed mode
+J's density contraction also runs on the tensor cores (max|dJ| <= 1e-9);
+a J-only call takes the FP64 path."""
 import numpy as np
 import pytest
 
@@ -31,8 +32,22 @@ def test_split_k_vs_oracle(sysname, request):
     Jr = O.df_j(ds.Vinv, 2 * P, 1e-10)
     dK = np.abs(K - Kr).max()
     print(f"{sysname}: max|dK| = {dK:.3e}  max|K| = {np.abs(Kr).max():.3f}")
+    # mixed-mode J: density contracted on the tensor cores against L^-1 B,
+    # then one FP64 pass over L^-1 B (no V^-1 in the path).  Its split error
+    # is measured against the same Cholesky-route formula in FP64; the
+    # V^-1-route FP64 J carries its own ~1e-9 rounding noise (cond(V) ~ 1e7)
+    T = ds.layout.to_dense(ds.B)
+    Bt = np.einsum("yx,xmn->ymn", np.tril(ds.Linv), T)
+    Jc = np.einsum("y,ymn->mn", np.einsum("ymn,mn->y", Bt, 2 * P), Bt)
+    dJ = np.abs(J - Jc).max()
+    print(f"{sysname}: max|dJ| = {dJ:.3e} (Cholesky route), "
+          f"{np.abs(J - Jr).max():.3e} (V^-1 route)  max|J| = {np.abs(Jr).max():.3f}")
     assert dK <= 1e-9
-    assert np.array_equal(J, Jr)
+    assert dJ <= 1e-9
+    assert np.abs(J - Jr).max() <= 1e-8
+    # J alone (no coefficients) takes the FP64 path: identical to the oracle
+    Jalone, _ = eng.compute_jk(2 * P, None)
+    assert np.array_equal(Jalone, Jr)
     # repeated builds are deterministic
     _, K2 = eng.compute_jk(None, C, "dfmo")
     assert np.array_equal(K, K2)
