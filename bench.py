@@ -69,6 +69,7 @@ def workload_config(ds, mol, nC, precision, world):
         "kept_block_pairs": round(ds.layout.kept_block_fraction(), 4),
         "precision": precision, "kmethod": "dfmo", "jmethod": "dfao",
         "l2_flush": "none: resident 3-center tensor (%.2f GB) exceeds L2" % (ds.layout.nnz * 8e-9),
+        "launch": "whole build replayed as one CUDA graph",
         "parallelism": f"replicas x{world}",
     }
 
@@ -199,9 +200,12 @@ def main():
     torch.cuda.synchronize()
     stream = torch.cuda.ExternalStream(eng.stream, device=dev)
 
+    # the whole Fock build (all launches, memsets) is one CUDA graph
+    eng.capture_graph(dP.data_ptr(), dC.data_ptr(), mol.nocc, dJ.data_ptr(), dK.data_ptr(),
+                      args.kmethod)
+
     def step():
-        eng.compute_jk_dev(dP.data_ptr(), dC.data_ptr(), mol.nocc, dJ.data_ptr(), dK.data_ptr(),
-                           args.kmethod)
+        eng.launch_graph()
 
     for _ in range(max(3, args.warmup)):
         step()
@@ -229,10 +233,12 @@ def main():
         ms = float(t.item())
     value = world * 1e3 / ms
 
-    # per-phase device time (CUDA events around every launch), same steps
+    # per-phase device time (CUDA events around every launch), same builds
+    # issued directly rather than through the graph
     eng.profile(True)
     for _ in range(args.steps):
-        step()
+        eng.compute_jk_dev(dP.data_ptr(), dC.data_ptr(), mol.nocc, dJ.data_ptr(), dK.data_ptr(),
+                           args.kmethod)
     eng.synchronize()
     prof = eng.profile_read()
     eng.profile(False)
@@ -272,8 +278,13 @@ def main():
     if name.startswith("split_gemm"):
         f = pairs * flops64[name]
         ach = f / (per_launch_ms * 1e-3) / 1e12
+        # DRAM bytes per launch of the half transform from the ncu capture in
+        # profiles/k_split_gemm_c14h30.md (2.045 GB for 1.6618e8 tensor
+        # elements), scaled by the tensor elements of this workload
+        traffic = 2.045e9 / 1.6618e8 * nnz if name == "split_gemm_ht" else None
         roof = {"kernel": "k_split_gemm (" + name + ")", "bound": "tensor", "achieved": ach,
-                "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16, "traffic": None,
+                "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16, "traffic": traffic,
+                "traffic_source": "ncu capture on C14H30 scaled by tensor elements",
                 "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)",
                 "algorithmic_flops_per_launch": f,
                 "flops_definition": "15 BF16 digit-pair products x 2*M*N*K of the unpadded "
@@ -306,11 +317,15 @@ def main():
         f1 = torch.cuda.Event(enable_timing=True)
         f0.record(stream)
         for _ in range(nst):
-            step()
+            eng.compute_jk_dev(dP.data_ptr(), dC.data_ptr(), mol.nocc, dJ.data_ptr(),
+                               dK.data_ptr(), args.kmethod)
         f1.record(stream)
         torch.cuda.synchronize()
         ms64 = f0.elapsed_time(f1) / nst
         Jf, Kf = eng.compute_jk(Ph, Cocc, args.kmethod)
+        eng.set_jmode("cholesky")
+        Jfc, _ = eng.compute_jk(Ph, None, args.kmethod)
+        eng.set_jmode("vinv")
         eng.set_precision(args.precision)
         fp64 = {"value": world * 1e3 / ms64, "unit": "builds/s", "ms_per_step": ms64,
                 "steps": nst,
@@ -319,6 +334,11 @@ def main():
                 "max_abs_dJ": float(np.abs(Jm - Jf).max()),
                 "dE_Eh": float(np.sum(P * ((Jm - Jf) + (Km - Kf)))),
                 "dE_K_Eh": float(np.sum(P * (Km - Kf))),
+                "max_abs_dJ_vs_fp64_cholesky": float(np.abs(Jm - Jfc).max()),
+                "dE_vs_fp64_cholesky_Eh": float(np.sum(P * ((Jm - Jfc) + (Km - Kf)))),
+                "fp64_route_note": "fp64 J uses the explicit V^-1 of fock::DF_J; for this "
+                                   "metric (cond ~2e7) that route itself errs by ~1e-6 Eh in "
+                                   "the Coulomb energy, the Cholesky route by ~1e-10 Eh",
                 "dE_definition": "sum P_alpha ((J + K)_mixed - (J + K)_fp64): energy change "
                                  "of one Fock build at the bench density (E = sum P_alpha "
                                  "(H + F), F = H + J + K)"}

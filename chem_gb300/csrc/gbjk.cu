@@ -76,7 +76,8 @@ struct gbjk_ctx {
   bool colsum_smem_set = false;
   // J workspace
   double *d_P = nullptr, *d_Pg = nullptr, *d_part = nullptr, *d_g = nullptr, *d_h = nullptr,
-         *d_J = nullptr;
+         *d_y = nullptr, *d_J = nullptr;
+  int jmode = GBJK_J_VINV;
   // K workspace (per nocc)
   int ws_nocc = -1;
   int ksplit = 1;
@@ -99,6 +100,10 @@ struct gbjk_ctx {
   int64_t ph_launch[PH_COUNT] = {};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
   std::vector<cudaEvent_t> ev_pool;
+  // captured Fock build
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_launch_count = 0;
 };
 
 namespace {
@@ -353,6 +358,7 @@ gbjk_status ensure_j_workspace(gbjk_ctx* ctx) {
   if ((s = dalloc(ctx, &ctx->d_part, nbf * naux))) return s;
   if ((s = dalloc(ctx, &ctx->d_g, naux))) return s;
   if ((s = dalloc(ctx, &ctx->d_h, naux))) return s;
+  if ((s = dalloc(ctx, &ctx->d_y, naux))) return s;
   if ((s = dalloc(ctx, &ctx->d_J, nbf * nbf))) return s;
   if ((s = dalloc(ctx, &ctx->d_K, nbf * nbf))) return s;
   return GBJK_OK;
@@ -405,8 +411,17 @@ gbjk_status run_j(gbjk_ctx* ctx, const double* dP, double* dJ) {
   }
   {
     PhaseScope ps(ctx, PH_J_METRIC);
-    k_gemv<<<cdiv((long long)naux * 32, 256), 256, 0, ctx->stream>>>(ctx->d_Vinv, ctx->d_g, naux,
-                                                                       ctx->d_h);
+    if (ctx->jmode == GBJK_J_CHOLESKY) {
+      // h = L^-T (L^-1 g): no explicit V^-1
+      k_gemv<<<cdiv((long long)naux * 32, 256), 256, 0, ctx->stream>>>(ctx->d_Linv, ctx->d_g,
+                                                                         naux, ctx->d_y);
+      CKL(PH_J_METRIC);
+      k_gemv_lower_t<<<cdiv(naux, 128), 128, 0, ctx->stream>>>(ctx->d_Linv, ctx->d_y, naux,
+                                                               ctx->d_h);
+    } else {
+      k_gemv<<<cdiv((long long)naux * 32, 256), 256, 0, ctx->stream>>>(ctx->d_Vinv, ctx->d_g,
+                                                                         naux, ctx->d_h);
+    }
     CKL(PH_J_METRIC);
   }
   {
@@ -559,7 +574,7 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   ctx->split.release();
   void* ptrs[] = {ctx->d_blk_of, ctx->d_boff,  ctx->d_panelK, ctx->d_cmoff, ctx->d_colmap,
                   ctx->d_panel_off, ctx->d_pg_off, ctx->d_B, ctx->d_Linv, ctx->d_Vinv,
-                  ctx->d_P, ctx->d_Pg, ctx->d_part, ctx->d_g, ctx->d_h, ctx->d_J,
+                  ctx->d_P, ctx->d_Pg, ctx->d_part, ctx->d_g, ctx->d_h, ctx->d_y, ctx->d_J,
                   ctx->d_C, ctx->d_Cg, ctx->d_H, ctx->d_H2, ctx->d_Kpart, ctx->d_K,
                   ctx->d_groups, ctx->d_tiles};
   for (void* p : ptrs)
@@ -569,6 +584,8 @@ void gbjk_destroy(gbjk_ctx* ctx) {
     cudaEventDestroy(pe.second.second);
   }
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
+  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
+  if (ctx->graph) cudaGraphDestroy(ctx->graph);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -609,6 +626,14 @@ gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices) {
     return fail(ctx, GBJK_INVALID_ARG, "nslices out of range");
   ctx->precision = precision;
   ctx->nslices = nslices;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (jmode != GBJK_J_VINV && jmode != GBJK_J_CHOLESKY)
+    return fail(ctx, GBJK_INVALID_ARG, "unknown J mode");
+  ctx->jmode = jmode;
   return GBJK_OK;
 }
 
@@ -693,6 +718,52 @@ gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, co
   }
   if (dJ && (s = run_j(ctx, dP, dJ))) return s;
   if (dK && (s = run_k(ctx, kmethod, dC, nocc, dK))) return s;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_capture_graph(gbjk_ctx* ctx, int kmethod, const double* dP, const double* dC,
+                               int nocc, double* dJ, double* dK) {
+  gbjk_status s;
+  if (!ctx) return GBJK_INVALID_ARG;
+  // one ordinary build prepares every plan, buffer and kernel attribute so
+  // that the captured sequence contains launches and memsets only
+  if ((s = gbjk_compute_jk_dev(ctx, kmethod, dP, dC, nocc, dJ, dK))) return s;
+  if ((s = gbjk_synchronize(ctx))) return s;
+  const bool prof = ctx->profile;
+  ctx->profile = false;
+  ctx->split.profile = false;
+  if (ctx->graph_exec) {
+    cudaGraphExecDestroy(ctx->graph_exec);
+    ctx->graph_exec = nullptr;
+  }
+  if (ctx->graph) {
+    cudaGraphDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  const int64_t l0 = ctx->launches;
+  s = gbjk_compute_jk_dev(ctx, kmethod, dP, dC, nocc, dJ, dK);
+  ctx->graph_launch_count = ctx->launches - l0;
+  ctx->launches = l0;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->profile = prof;
+  ctx->split.profile = prof;
+  if (s) {
+    if (g) cudaGraphDestroy(g);
+    return s;
+  }
+  if (e != cudaSuccess) return fail(ctx, GBJK_CUDA_ERROR, std::string("graph capture: ") + cudaGetErrorString(e));
+  ctx->graph = g;
+  CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_launch_graph(gbjk_ctx* ctx) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (!ctx->graph_exec) return fail(ctx, GBJK_NOT_READY, "no captured build");
+  CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
+  ctx->launches += ctx->graph_launch_count;
   return GBJK_OK;
 }
 

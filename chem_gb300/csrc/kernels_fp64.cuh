@@ -83,6 +83,17 @@ __global__ void k_gemv(const double* __restrict__ M, const double* __restrict__ 
   if (lane == 0) y[row] = s;
 }
 
+// y = L^T x for lower-triangular L (n x n row-major): y[X] = sum_{Y >= X}
+// L[Y][X] x[Y], one thread per X, in increasing Y.
+__global__ void k_gemv_lower_t(const double* __restrict__ L, const double* __restrict__ x, int n,
+                               double* __restrict__ y) {
+  const int X = blockIdx.x * blockDim.x + threadIdx.x;
+  if (X >= n) return;
+  double s = 0.0;
+  for (int Y = X; Y < n; ++Y) s = fma(L[(long long)Y * n + X], x[Y], s);
+  y[X] = s;
+}
+
 // J[mu][colmap[k]] = sum_X B_I[m][X][k] h[X]; grid (ceil(maxK/128), nbf).
 __global__ void k_j_colsum(const double* __restrict__ B, const long long* __restrict__ panel_off,
                            const int* __restrict__ blk_of, const int* __restrict__ boff,

@@ -334,7 +334,32 @@ struct SplitState {
     const long long hk = (long long)naux * hld;
     h_nkt = cdiv_(hk, kTileK);
     h_nrb = std::max(cdiv_(nbf, kTileM) * (kTileM / 32), cdiv_(nbf, kTileN) * (kTileN / 32));
-    const int kt_per = 256;  // at most 8192 k per exchange item
+    // split-K of the exchange: items of at most 256 k-tiles (8192 k, the
+    // int64 headroom of the exact accumulator), count chosen to fill whole
+    // waves of persistent CTAs (one CTA per SM)
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int ntile = 0;
+    for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
+      for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt)
+        if ((nt + 1) * kTileN > mt * kTileM) ++ntile;
+    {
+      const int ks_min = cdiv_(h_nkt, 256);
+      double best = 1e300;
+      ksplit = ks_min;
+      for (int ks = ks_min; ks <= std::max(ks_min, 4 * nsm); ++ks) {
+        const int per = cdiv_(h_nkt, ks);
+        if (per < 8 && ks > ks_min) break;
+        const long long waves = ((long long)ntile * ks + nsm - 1) / nsm;
+        const double t = (double)waves * (per + 2.0);  // +2: per-item overhead in k-tiles
+        if (t < best) {
+          best = t;
+          ksplit = ks;
+        }
+      }
+    }
+    const int kt_per = cdiv_(h_nkt, ksplit);
     ksplit = cdiv_(h_nkt, kt_per);
     if (alloc(&d_Cslices, (size_t)ctot) != cudaSuccess ||
         alloc(&d_eC, (size_t)nblk * c_nrb * 32) != cudaSuccess ||

@@ -56,12 +56,16 @@ def lib():
         L.gbjk_upload_b.argtypes = [vp, dp]
         L.gbjk_upload_metric.argtypes = [vp, dp, dp]
         L.gbjk_set_precision.argtypes = [vp, C.c_int, C.c_int]
+        L.gbjk_set_jmode.argtypes = [vp, C.c_int]
         L.gbjk_compute_j.argtypes = [vp, dp, dp]
         L.gbjk_compute_k.argtypes = [vp, C.c_int, dp, C.c_int, dp]
         L.gbjk_compute_jk.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, dp]
         L.gbjk_compute_jk_dev.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                           C.c_void_p, C.c_void_p]
         L.gbjk_synchronize.argtypes = [vp]
+        L.gbjk_capture_graph.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
+                                         C.c_void_p, C.c_void_p]
+        L.gbjk_launch_graph.argtypes = [vp]
         L.gbjk_stream.argtypes = [vp]
         L.gbjk_stream.restype = C.c_void_p
         L.gbjk_device_bytes.argtypes = [vp]
@@ -133,6 +137,11 @@ class JKEngine:
                     "gbjk_set_precision")
         self.precision = precision
 
+    def set_jmode(self, jmode):
+        """'vinv' (reference route, default) or 'cholesky'."""
+        code = {"vinv": 0, "cholesky": 1}[jmode]
+        self._check(lib().gbjk_set_jmode(self.h, code), "gbjk_set_jmode")
+
     def compute_jk(self, Ptot=None, Cocc=None, kmethod="dfmo"):
         n = self.nbf
         J = np.zeros((n, n)) if Ptot is not None else None
@@ -151,6 +160,14 @@ class JKEngine:
         """Device pointers (ints); ordered on the engine stream, no sync."""
         self._check(lib().gbjk_compute_jk_dev(self.h, KMETHODS[kmethod], dP, dC, int(nocc),
                                               dJ, dK), "gbjk_compute_jk_dev")
+
+    def capture_graph(self, dP, dC, nocc, dJ, dK, kmethod="dfmo"):
+        """Capture one device-pointer build as a CUDA graph (see gbjk.h)."""
+        self._check(lib().gbjk_capture_graph(self.h, KMETHODS[kmethod], dP, dC, int(nocc),
+                                             dJ, dK), "gbjk_capture_graph")
+
+    def launch_graph(self):
+        self._check(lib().gbjk_launch_graph(self.h), "gbjk_launch_graph")
 
     def synchronize(self):
         self._check(lib().gbjk_synchronize(self.h), "gbjk_synchronize")

@@ -53,6 +53,14 @@ typedef enum { GBJK_FP64 = 0, GBJK_SPLIT_BF16 = 1 } gbjk_precision;
 /* K builder, by the reference's kmethod strings (src/fock/jkbuilder.hpp:37-60) */
 typedef enum { GBJK_K_DFMO = 0, GBJK_K_DFLMO = 1 } gbjk_kmethod;
 
+/* Route of the FP64 J's metric step.  GBJK_J_VINV multiplies by the
+ * explicit inverse V^-1 = L^-T L^-1, as fock::DF_J does
+ * (src/fock/jkdf.cpp:137-141).  GBJK_J_CHOLESKY applies L^-1 and then
+ * L^-T; for an ill-conditioned Coulomb metric (cond ~1e7 for C20H42 /
+ * cc-pVDZ-jkfit) it is several orders of magnitude more accurate.  The mixed
+ * path always uses the Cholesky route. */
+typedef enum { GBJK_J_VINV = 0, GBJK_J_CHOLESKY = 1 } gbjk_jmode;
+
 typedef struct gbjk_ctx gbjk_ctx;
 
 /* Atom-block panel layout of the 3-center tensor (X|mu nu):
@@ -84,6 +92,10 @@ gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* 
  * operand for the split path (ignored for FP64; 0 picks the default). */
 gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices);
 
+/* jmode: GBJK_J_VINV (default, the reference route) or GBJK_J_CHOLESKY.
+ * No counterpart in the reference. */
+gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode);
+
 /* J_{mu nu} = sum_X (X|mu nu) [V^-1 g]_X, g_X = sum (X|mu nu) Ptot_{mu nu}. */
 gbjk_status gbjk_compute_j(gbjk_ctx* ctx, const double* Ptot, double* J);
 /* K_{mu nu} = -sum_{X,i} Bfit_{X mu i} Bfit_{X nu i}, Cocc is nbf x nocc. */
@@ -96,6 +108,13 @@ gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* Ptot, cons
 gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dPtot,
                                 const double* dCocc, int nocc, double* dJ, double* dK);
 gbjk_status gbjk_synchronize(gbjk_ctx* ctx);
+/* Capture one device-pointer Fock build (same arguments as
+ * gbjk_compute_jk_dev) as a CUDA graph on the context's stream, after one
+ * ordinary build that prepares every plan; gbjk_launch_graph replays it
+ * (same pointers, new contents).  No counterpart in the reference. */
+gbjk_status gbjk_capture_graph(gbjk_ctx* ctx, int kmethod, const double* dPtot,
+                               const double* dCocc, int nocc, double* dJ, double* dK);
+gbjk_status gbjk_launch_graph(gbjk_ctx* ctx);
 /* The context's cudaStream_t, as void*. */
 void* gbjk_stream(gbjk_ctx* ctx);
 

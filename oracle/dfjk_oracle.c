@@ -13,6 +13,7 @@
  *
  * Functions and the reference code they restate:
  *   oracle_df_j      fock::DF_J::compute_J      src/fock/jkdf.cpp:69-190
+ *   oracle_df_j_chol the same J with the metric applied as L^-T L^-1
  *   oracle_dfmo_k    fock::DFMO_K::compute_K    src/fock/jkdf.cpp:221-462
  *   oracle_dflmo_k   fock::DFLMO_K::compute_K   src/fock/jkdf.cpp:897-1091
  *                    (symmetric branch)
@@ -153,6 +154,32 @@ void oracle_df_j(const oracle_layout* L, const double* B, const double* Vinv,
   oracle_contract_j(L, B, h, J);
   oracle_filter(L, J, eps);
   free(g);
+  free(h);
+}
+
+/* DF-J through the Cholesky factor: h = L^-T (L^-1 g), with y = L^-1 g as
+ * warp dots over the rows of L^-1 and h[X] = sum_{Y >= X} L^-1[Y][X] y[Y]
+ * in increasing Y.  Same value as oracle_df_j in exact arithmetic; avoids
+ * the conditioning error of the explicit V^-1. */
+void oracle_df_j_chol(const oracle_layout* L, const double* B, const double* Linv,
+                      const double* Ptot, double* J, double eps) {
+  const int naux = L->naux;
+  double* g = (double*)malloc(sizeof(double) * naux);
+  double* y = (double*)malloc(sizeof(double) * naux);
+  double* h = (double*)malloc(sizeof(double) * naux);
+  oracle_contract_g(L, B, Ptot, g);
+#pragma omp parallel for schedule(static)
+  for (int Y = 0; Y < naux; ++Y) y[Y] = warp_dot(Linv + (size_t)Y * naux, g, naux, 1);
+#pragma omp parallel for schedule(static)
+  for (int X = 0; X < naux; ++X) {
+    double s = 0.0;
+    for (int Y = X; Y < naux; ++Y) s = fma(Linv[(size_t)Y * naux + X], y[Y], s);
+    h[X] = s;
+  }
+  oracle_contract_j(L, B, h, J);
+  oracle_filter(L, J, eps);
+  free(g);
+  free(y);
   free(h);
 }
 

@@ -50,6 +50,7 @@ def lib():
         dp = C.POINTER(C.c_double)
         lp = C.POINTER(OracleLayout)
         L.oracle_df_j.argtypes = [lp, dp, dp, dp, dp, C.c_double]
+        L.oracle_df_j_chol.argtypes = [lp, dp, dp, dp, dp, C.c_double]
         L.oracle_dfmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
         L.oracle_dflmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
         L.oracle_dfao_k.argtypes = [lp, dp, dp, dp, dp, C.c_double]
@@ -88,6 +89,13 @@ class Oracle:
         J = np.zeros((n, n))
         lib().oracle_df_j(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Vinv)),
                           _dp(np.ascontiguousarray(Ptot)), _dp(J), eps)
+        return J
+
+    def df_j_chol(self, Linv, Ptot, eps=0.0):
+        n = self.layout.nbf
+        J = np.zeros((n, n))
+        lib().oracle_df_j_chol(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Linv)),
+                               _dp(np.ascontiguousarray(Ptot)), _dp(J), eps)
         return J
 
     def dfmo_k(self, Linv, Cocc, eps=0.0, kchunk=0):

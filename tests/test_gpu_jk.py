@@ -91,3 +91,17 @@ def test_empty_filter_eps_zero(water):
     kc = k_split_plan(ds.nbf, ds.naux, ds.nocc)[1]
     assert np.array_equal(J, O.df_j(ds.Vinv, 2 * C @ C.T, 0.0))
     assert np.array_equal(K, O.dfmo_k(np.tril(ds.Linv), C, 0.0, kchunk=kc))
+
+
+@pytest.mark.parametrize("sysname", ["water", "butane", "decane"])
+def test_fp64_cholesky_route_bitwise(sysname, request):
+    ds = request.getfixturevalue(sysname)
+    eng = _engine(ds)
+    eng.set_jmode("cholesky")
+    O = Oracle(ds.layout, ds.B)
+    C = _orbitals(ds)
+    P = C @ C.T
+    J, _ = eng.compute_jk(2 * P, None)
+    Jr = O.df_j_chol(np.tril(ds.Linv), 2 * P, 1e-10)
+    assert np.array_equal(J, Jr)
+    eng.close()

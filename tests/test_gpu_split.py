@@ -45,6 +45,13 @@ def test_split_k_vs_oracle(sysname, request):
     assert dK <= 1e-9
     assert dJ <= 1e-9
     assert np.abs(J - Jr).max() <= 1e-8
+    # and against the device FP64 path on the Cholesky route
+    eng.set_precision("fp64")
+    eng.set_jmode("cholesky")
+    J64c, _ = eng.compute_jk(2 * P, None)
+    assert np.abs(J - J64c).max() <= 1e-9
+    eng.set_jmode("vinv")
+    eng.set_precision("split")
     # J alone (no coefficients) takes the FP64 path: identical to the oracle
     Jalone, _ = eng.compute_jk(2 * P, None)
     assert np.array_equal(Jalone, Jr)
