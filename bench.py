@@ -40,6 +40,7 @@ def parse():
     ap.add_argument("--alkane", type=int, default=20)
     ap.add_argument("--kmethod", default="dfmo")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-scf", action="store_true")
     return ap.parse_args()
 
 
@@ -343,6 +344,50 @@ def main():
                                  "of one Fock build at the bench density (E = sum P_alpha "
                                  "(H + F), F = H + J + K)"}
 
+    # full DF-HF SCF (the config's SCF comparison): FP64 on the reference
+    # route, FP64 on the Cholesky route, mixed precision switching to FP64
+    # (Cholesky route) once the DIIS error is below 1e-5
+    scf = None
+    if not args.no_scf:
+        from chem_gb300.scf import run_rhf
+
+        def run(prec, jmode, switch):
+            eng.set_precision(prec)
+            eng.set_jmode(jmode)
+
+            def jk(Pa, Ca):
+                return eng.compute_jk(2.0 * Pa, Ca, args.kmethod)
+
+            sw = None
+            if switch:
+                def sw():
+                    eng.set_precision("fp64")
+            t0 = time.perf_counter()
+            r = run_rhf(ds.S, ds.Hcore, mol.nuclear_repulsion(), mol.nocc, jk, conv=1e-8,
+                        switch=sw)
+            return r, time.perf_counter() - t0
+
+        r_ref, t_ref = run("fp64", "vinv", False)
+        r_chol, t_chol = run("fp64", "cholesky", False)
+        r_mix, t_mix = run("split", "cholesky", True)
+        r_pure, t_pure = run("split", "cholesky", False)
+        eng.set_precision(args.precision)
+        eng.set_jmode("vinv")
+        scf = {"conv_rms": 1e-8,
+               "fp64_vinv_route": {"E": r_ref.energy, "iterations": r_ref.iterations,
+                                   "seconds": round(t_ref, 2), "converged": r_ref.converged},
+               "fp64_cholesky_route": {"E": r_chol.energy, "iterations": r_chol.iterations,
+                                       "seconds": round(t_chol, 2),
+                                       "converged": r_chol.converged},
+               "mixed_then_fp64": {"E": r_mix.energy, "iterations": r_mix.iterations,
+                                   "seconds": round(t_mix, 2), "converged": r_mix.converged,
+                                   "switch": "FP64 once the DIIS RMS error < 1e-5"},
+               "mixed_only": {"E": r_pure.energy, "iterations": r_pure.iterations,
+                              "seconds": round(t_pure, 2), "converged": r_pure.converged},
+               "dE_mixed_only_vs_fp64_cholesky": r_pure.energy - r_chol.energy,
+               "dE_mixed_then_fp64_vs_fp64_cholesky": r_mix.energy - r_chol.energy,
+               "dE_fp64_vinv_vs_cholesky": r_ref.energy - r_chol.energy}
+
     out = {
         "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -357,6 +402,7 @@ def main():
         "gpu_launches": int(launches),
         "roofline": roof,
         "fp64_gpu": fp64,
+        "scf": scf,
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[1]},
         "clocks": clk.summary(),
         "setup_s": {"integrals_host": round(tset, 2)},

@@ -5,8 +5,9 @@ Restates the parts of megalochem's hf::hfmod the configs need:
   * form_fock: F = H + J + K_A with J from P_tot = 2 P_A and K_A already
     negated (src/hf/hfscf.cpp:228-276);
   * energy E = sum P_A (H + F) + E_nuc (src/hf/hfscf.cpp:278-296);
-  * error matrix FPS - SPF in the orthogonal basis and its RMS
-    (src/hf/hfscf.cpp:298-324, :381-384);
+  * error matrix FPS - SPF (AO basis) and its RMS sqrt(sum e^2 / nbf^2);
+    converged when the RMS falls below the threshold after the first
+    iteration (src/hf/hfscf.cpp:298-324, :381-384, :430);
   * DIIS extrapolation on the Fock matrices (src/math/solvers/diis.hpp:43-234);
   * diagonalisation X^T F X and P = C_occ C_occ^T (src/hf/hfdiagfock.cpp:20-102).
 The guess is the core Hamiltonian (megalochem's default SAD guess runs an
@@ -65,7 +66,8 @@ class DIIS:
 
 def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max_vecs=8,
             switch=None, switch_thresh=1e-5, log=None):
-    """jk(P_alpha, C_occ) -> (J, K_alpha) with K already negated.
+    """jk(P_alpha, C_occ) -> (J, K_alpha) with K already negated; conv is the
+    RMS threshold of the error matrix (megalochem's scf_thresh).
     switch(): called once when the DIIS RMS error falls below switch_thresh
     (moves a split-precision engine to FP64)."""
     s, U = np.linalg.eigh(S)
@@ -84,7 +86,7 @@ def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max
         J, K = jk(P, Cocc)
         F_new = Hcore + J + K
         E = float(np.sum(P * (Hcore + F_new)) + enuc)
-        err = X.T @ (F_new @ P @ S - S @ P @ F_new) @ X
+        err = F_new @ P @ S - S @ P @ F_new
         rms = float(np.sqrt(np.mean(err ** 2)))
         hist.append((it, E, E - E_old, rms))
         if log:
@@ -95,7 +97,7 @@ def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max
             E_old = E
             F = F_new
             continue
-        if it > 0 and abs(E - E_old) < conv and rms < np.sqrt(conv) and switched:
+        if it > 0 and rms < conv and switched:
             return SCFResult(E, True, it + 1, Cm, e, P, F_new, hist)
         E_old = E
         if it >= diis_start:
