@@ -1,0 +1,296 @@
+"""Continuous-batching Fock-build server on one GPU.
+
+A request asks for the Fock-build contractions (J, K) of one molecule at one
+density.  The server keeps every admitted molecule resident on the device as
+a J/K engine (its 3-center tensor, metric factors, digit slices and
+workspaces) and serves requests as they arrive:
+
+* set-up — the host integrals of a molecule not seen before run on a CPU
+  pipeline (one job at a time, each using all host threads);
+* admission — a molecule's engine is created when its device footprint fits
+  the HBM budget; idle engines are evicted least-recently-used to make room;
+  a request waits until its engine is resident and a GPU slot is free;
+* execution — GPU slots are host threads, each issuing builds on its own
+  engine's CUDA stream, so builds of different molecules overlap on the
+  device; a molecule's builds are serialised on its engine.
+Every build runs the same deterministic kernels whatever else is in flight,
+so a result in the mix is bit-identical to the same request served alone.
+
+megalochem has no serving layer; its SCF loop calls the builders in-process
+(src/hf/hfscf.cpp:241-259).  This module is the multi-request caller of the
+same boundary.
+"""
+from __future__ import annotations
+
+import heapq
+import threading
+import time
+from collections import OrderedDict
+from concurrent.futures import ThreadPoolExecutor
+from dataclasses import dataclass, field
+
+import numpy as np
+
+
+@dataclass
+class Request:
+    rid: int
+    key: str             # molecule identity
+    arrival: float       # seconds after the start of the run
+    make_system: object  # callable() -> (DFSystem, P_alpha, C_occ)
+    t_setup_done: float = None
+    t_admitted: float = None
+    t_done: float = None
+    J: np.ndarray = None
+    K: np.ndarray = None
+    error: str = None
+
+    @property
+    def latency(self):
+        return None if self.t_done is None else self.t_done - self.arrival
+
+
+def footprint_bytes(layout, nocc, precision="split"):
+    """Device bytes a J/K engine will hold for this molecule (estimate used
+    for admission; the engine's own gbjk_device_bytes is recorded after)."""
+    nnz, nbf, naux = layout.nnz, layout.nbf, layout.naux
+    b = 8 * nnz + 2 * 8 * naux * naux           # B, L^-1, V^-1
+    b += 8 * (nbf * nbf * 4 + nbf * naux)       # P, J, K, partials
+    if precision == "split":
+        b += 8 * nnz + 11 * nnz                 # L^-1 B (FP64) + digit slices (padded)
+        b += 8 * nbf * naux * (nocc + 1)        # fitted half transform
+        b += 11 * nbf * naux * (nocc + 1)       # its digits
+        b += 8 * nbf * nbf * 64                 # split-K partials (upper bound)
+    else:
+        b += 2 * 8 * nbf * naux * nocc + 8 * nbf * nbf * 64
+    return int(b * 1.05) + (64 << 20)
+
+
+class _Resident:
+    def __init__(self, engine, nbytes):
+        self.engine = engine
+        self.nbytes = nbytes
+        self.lock = threading.Lock()
+        self.busy = 0
+        self.measured = False
+
+
+class FockServer:
+    """Serves Request objects; see the module docstring."""
+
+    def __init__(self, budget_bytes=150e9, slots=8, precision="split", device=0,
+                 engine_factory=None, clock=time.perf_counter, drop_host_tensor=True):
+        self.budget = int(budget_bytes)
+        self.drop_host_tensor = drop_host_tensor
+        self.slots = slots
+        self.precision = precision
+        self.device = device
+        self.clock = clock
+        self._engine_factory = engine_factory or self._make_engine
+        self._cv = threading.Condition()
+        self._resident = OrderedDict()   # key -> _Resident (LRU order)
+        self._used = 0
+        self._systems = {}               # key -> (ds, P, C) once set up
+        self._setup_pending = {}         # key -> future
+        self._ready = []                 # heap of (arrival, rid, request)
+        self._cpu = ThreadPoolExecutor(1)
+        self.max_used = 0
+        self.builds = 0
+        self.log = []
+
+    # -- engines -------------------------------------------------------------
+    def _make_engine(self, ds):
+        from .fock import JKEngine
+        return JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=ds.eps,
+                        device=self.device, precision=self.precision)
+
+    def _evict_for(self, need):
+        """Evict idle engines (LRU first) until `need` bytes fit; caller holds _cv."""
+        for key in list(self._resident.keys()):
+            if self._used + need <= self.budget:
+                break
+            r = self._resident[key]
+            if r.busy:
+                continue
+            del self._resident[key]
+            self._used -= r.nbytes
+            r.engine.close()
+            self.log.append(("evict", key))
+        return self._used + need <= self.budget
+
+    def _acquire(self, req):
+        """Block until the request's engine is resident and reserved for it."""
+        ds, _, _ = self._systems[req.key]
+        need = footprint_bytes(ds.layout, ds.nocc, self.precision)
+        if need > self.budget:
+            raise RuntimeError(f"molecule {req.key} needs {need / 1e9:.1f} GB > budget")
+        with self._cv:
+            while True:
+                r = self._resident.get(req.key)
+                if r is not None:
+                    self._resident.move_to_end(req.key)
+                    r.busy += 1
+                    return r
+                if self._evict_for(need):
+                    self._used += need
+                    self.max_used = max(self.max_used, self._used)
+                    break
+                self._cv.wait()
+        if getattr(ds, "B", 1) is None:
+            # the host copy was dropped when an earlier engine took it: set
+            # the molecule up again (only after an eviction)
+            self._systems[req.key] = req.make_system()
+            ds = self._systems[req.key][0]
+        eng = self._engine_factory(ds)
+        if self.drop_host_tensor and hasattr(ds, "B"):
+            ds.B = None  # the engine holds the device copy
+        r = _Resident(eng, need)
+        r.busy = 1
+        with self._cv:
+            self._resident[req.key] = r
+            self.log.append(("admit", req.key))
+            self._cv.notify_all()
+        return r
+
+    def _true_up(self, r):
+        """After an engine's first build (all its buffers allocated), replace
+        the admission estimate by its measured device bytes."""
+        r.measured = True
+        actual = getattr(r.engine, "device_bytes", None)
+        if actual is None:
+            return
+        actual = int(actual * 1.02) + (16 << 20)
+        if actual < r.nbytes:
+            with self._cv:
+                self._used -= r.nbytes - actual
+                r.nbytes = actual
+                self._cv.notify_all()
+
+    def _release(self, r):
+        with self._cv:
+            r.busy -= 1
+            self._cv.notify_all()
+
+    # -- request flow ----------------------------------------------------------
+    def _setup(self, req):
+        if req.key not in self._systems:
+            self._systems[req.key] = req.make_system()
+
+    def _on_setup(self, req, t0):
+        req.t_setup_done = self.clock() - t0
+        with self._cv:
+            heapq.heappush(self._ready, (req.arrival, req.rid, req))
+            self._cv.notify_all()
+
+    def _worker(self, t0, total):
+        while True:
+            with self._cv:
+                while not self._ready and self._done < total:
+                    self._cv.wait(0.05)
+                if self._done >= total and not self._ready:
+                    return
+                if not self._ready:
+                    continue
+                _, _, req = heapq.heappop(self._ready)
+            try:
+                r = self._acquire(req)
+                try:
+                    req.t_admitted = self.clock() - t0
+                    ds, P, C = self._systems[req.key]
+                    with r.lock:   # one build at a time per engine (its stream)
+                        req.J, req.K = r.engine.compute_jk(2.0 * P, C)
+                        if not r.measured:
+                            self._true_up(r)
+                finally:
+                    self._release(r)
+            except Exception as e:  # recorded, the server keeps serving
+                req.error = str(e)
+            req.t_done = self.clock() - t0
+            with self._cv:
+                self._done += 1
+                self.builds += req.error is None
+                self._cv.notify_all()
+
+    def run(self, requests, realtime=True):
+        """Serve `requests` (arrival times relative to now); returns them."""
+        reqs = sorted(requests, key=lambda q: q.arrival)
+        self._done = 0
+        t0 = self.clock()
+        workers = [threading.Thread(target=self._worker, args=(t0, len(reqs)), daemon=True)
+                   for _ in range(self.slots)]
+        for w in workers:
+            w.start()
+        futures = []
+        for req in reqs:
+            if realtime:
+                delay = req.arrival - (self.clock() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+            # set-up jobs run in arrival order on the CPU pipeline; later
+            # requests for the same molecule wait for the first one's job
+            fut = self._setup_pending.get(req.key)
+            if fut is None:
+                fut = self._cpu.submit(self._setup, req)
+                self._setup_pending[req.key] = fut
+            fut.add_done_callback(lambda _f, q=req: self._on_setup(q, t0))
+            futures.append(fut)
+        for w in workers:
+            w.join()
+        return reqs
+
+    def close(self):
+        with self._cv:
+            for r in self._resident.values():
+                r.engine.close()
+            self._resident.clear()
+            self._used = 0
+        self._cpu.shutdown(wait=True)
+
+
+def latency_stats(requests):
+    lat = np.array([q.latency for q in requests if q.error is None])
+    if lat.size == 0:
+        return {}
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "mean_s": float(lat.mean()), "max_s": float(lat.max()), "n": int(lat.size)}
+
+
+def make_system_factory(kind, size, eps=1e-10, basis="cc-pvdz", dfbasis="cc-pvdz-jkfit"):
+    """Callable building (DFSystem, P_alpha, C_occ) for an alkane C_nH_{2n+2}
+    (kind 'alkane', size n) or a water cluster (kind 'water', size k) at the
+    core-guess density.  Water-cluster geometries are seeded by k, so
+    requests of one cluster size share the molecule (and its set-up)."""
+    def make():
+        from . import geometry
+        from .dfsystem import build_dfsystem
+        from .molecule import molecule_from_angstrom
+        if kind == "alkane":
+            s, x = geometry.alkane(size)
+        else:
+            s, x = geometry.water_cluster(size, np.random.default_rng(1000 + size))
+        ds = build_dfsystem(molecule_from_angstrom(s, x, basis, dfbasis), eps=eps)
+        sv, U = np.linalg.eigh(ds.S)
+        X = U @ np.diag(sv ** -0.5) @ U.T
+        _, Cp = np.linalg.eigh(X.T @ ds.Hcore @ X)
+        C = np.ascontiguousarray((X @ Cp)[:, :ds.nocc])
+        return ds, C @ C.T, C
+    return make
+
+
+def poisson_requests(n, rate, seed, alkane=(4, 40), water=(2, 32)):
+    """n requests with exponential inter-arrival times (rate per second);
+    each is an alkane C_nH_{2n+2} (n uniform in `alkane`) or a water
+    cluster (k uniform in `water`), half and half."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for rid in range(n):
+        t += rng.exponential(1.0 / rate)
+        if rng.random() < 0.5:
+            size = int(rng.integers(alkane[0], alkane[1] + 1))
+            kind = "alkane"
+        else:
+            size = int(rng.integers(water[0], water[1] + 1))
+            kind = "water"
+        out.append(Request(rid, f"{kind}{size}", t, make_system_factory(kind, size)))
+    return out

@@ -1,0 +1,66 @@
+"""Admission, eviction and accounting of the Fock-build server, with a fake
+engine (no GPU): every admitted engine fits the HBM budget, idle engines
+are evicted least-recently-used, and every request is served."""
+import threading
+import time
+
+import numpy as np
+
+from chem_gb300.layout import build_layout
+from chem_gb300.serving import FockServer, Request, footprint_bytes
+
+
+class _DS:
+    def __init__(self, nbf, naux, nocc):
+        bs = [nbf // 2, nbf - nbf // 2]
+        self.layout = build_layout(bs, [naux], lambda I, J: np.ones(1, bool))
+        self.nocc = nocc
+        self.eps = 0.0
+
+
+class _FakeEngine:
+    live = 0
+    peak = 0
+    lock = threading.Lock()
+
+    def __init__(self, ds):
+        self.n = ds.layout.nbf
+        with _FakeEngine.lock:
+            _FakeEngine.live += 1
+            _FakeEngine.peak = max(_FakeEngine.peak, _FakeEngine.live)
+
+    def compute_jk(self, P, C):
+        time.sleep(0.002)
+        return P * 0 + 1.0, P * 0 - 1.0
+
+    def close(self):
+        with _FakeEngine.lock:
+            _FakeEngine.live -= 1
+
+
+def test_admission_and_eviction():
+    sizes = {"a": (40, 200, 5), "b": (60, 300, 7), "c": (80, 400, 9)}
+    systems = {k: (_DS(*v), np.eye(v[0]), np.ones((v[0], v[2]))) for k, v in sizes.items()}
+    fps = {k: footprint_bytes(s[0].layout, s[0].nocc) for k, s in systems.items()}
+    budget = fps["c"] + fps["b"]  # never all three at once
+    srv = FockServer(budget_bytes=budget, slots=3, engine_factory=_FakeEngine)
+    reqs = []
+    for i in range(30):
+        key = "abc"[i % 3]
+        reqs.append(Request(i, key, 0.001 * i, lambda k=key: systems[k]))
+    done = srv.run(reqs, realtime=True)
+    srv.close()
+    assert all(q.error is None for q in done)
+    assert all(np.all(q.J == 1.0) and np.all(q.K == -1.0) for q in done)
+    assert srv.max_used <= budget
+    assert _FakeEngine.peak <= 2
+    assert any(e[0] == "evict" for e in srv.log)
+    assert all(q.latency is not None and q.latency >= 0 for q in done)
+
+
+def test_oversized_request_is_an_error_not_a_hang():
+    ds = _DS(40, 200, 5)
+    srv = FockServer(budget_bytes=1000, slots=1, engine_factory=_FakeEngine)
+    done = srv.run([Request(0, "x", 0.0, lambda: (ds, np.eye(40), np.ones((40, 5))))])
+    srv.close()
+    assert done[0].error and "budget" in done[0].error
