@@ -73,6 +73,7 @@ struct gbjk_ctx {
   double* d_B = nullptr;
   double *d_Linv = nullptr, *d_Vinv = nullptr;
   bool have_B = false, have_metric = false;
+  bool fitted = false;  // the uploaded tensor already is L^-1 B (no metric)
   bool colsum_smem_set = false;
   // J workspace
   double *d_P = nullptr, *d_Pg = nullptr, *d_part = nullptr, *d_g = nullptr, *d_h = nullptr,
@@ -80,6 +81,7 @@ struct gbjk_ctx {
   int jmode = GBJK_J_VINV;
   // K workspace (per nocc)
   int ws_nocc = -1;
+  int wc_nocc = -1;
   int ksplit = 1;
   double *d_C = nullptr, *d_Cg = nullptr, *d_H = nullptr, *d_H2 = nullptr, *d_Kpart = nullptr,
          *d_K = nullptr;
@@ -213,13 +215,24 @@ void add_tiles(std::vector<GemmTile>& tiles, int group, int M, int N, int k0, in
     }
 }
 
-// (Re)build the K workspaces and launch plans for a given nocc.
+// Coefficient workspaces shared by both paths.
+gbjk_status ensure_c_workspace(gbjk_ctx* ctx, int nocc) {
+  if (ctx->wc_nocc == nocc) return GBJK_OK;
+  dfree(ctx, &ctx->d_C);
+  dfree(ctx, &ctx->d_Cg);
+  ctx->wc_nocc = -1;
+  gbjk_status s;
+  if ((s = dalloc(ctx, &ctx->d_C, (size_t)ctx->nbf * nocc))) return s;
+  if ((s = dalloc(ctx, &ctx->d_Cg, (size_t)ctx->ncols_total * nocc))) return s;
+  ctx->wc_nocc = nocc;
+  return GBJK_OK;
+}
+
+// (Re)build the FP64-path K workspaces and launch plans for a given nocc.
 gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
   if (ctx->ws_nocc == nocc) return GBJK_OK;
   const size_t nbf = ctx->nbf, naux = ctx->naux;
   const size_t hsz = nbf * naux * nocc;
-  dfree(ctx, &ctx->d_C);
-  dfree(ctx, &ctx->d_Cg);
   dfree(ctx, &ctx->d_H);
   dfree(ctx, &ctx->d_H2);
   dfree(ctx, &ctx->d_Kpart);
@@ -227,8 +240,7 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
   dfree(ctx, &ctx->d_tiles);
   ctx->ws_nocc = -1;
   gbjk_status s;
-  if ((s = dalloc(ctx, &ctx->d_C, nbf * nocc))) return s;
-  if ((s = dalloc(ctx, &ctx->d_Cg, (size_t)ctx->ncols_total * nocc))) return s;
+  if ((s = ensure_c_workspace(ctx, nocc))) return s;
   if ((s = dalloc(ctx, &ctx->d_H, hsz))) return s;
   if ((s = dalloc(ctx, &ctx->d_H2, hsz))) return s;
   // split-K of the exchange GEMM: enough tiles to fill the GPU
@@ -297,8 +309,8 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
   const int kchunk = (int)kchunk64;
   {
     GemmGroup g;
-    g.A = ctx->d_H2;
-    g.B = ctx->d_H2;
+    g.A = ctx->fitted ? ctx->d_H : ctx->d_H2;  // fitted tensor: H already carries L^-1
+    g.B = g.A;
     g.C = ctx->d_Kpart;
     g.M = (int)nbf;
     g.N = (int)nbf;
@@ -409,7 +421,10 @@ gbjk_status run_j(gbjk_ctx* ctx, const double* dP, double* dJ) {
     k_reduce_rows<<<cdiv(naux, 128), 128, 0, ctx->stream>>>(ctx->d_part, nbf, naux, ctx->d_g);
     CKL(PH_J_REDUCE);
   }
-  {
+  const double* hvec = ctx->d_h;
+  if (ctx->fitted) {
+    hvec = ctx->d_g;  // the tensor carries the metric: h = g
+  } else {
     PhaseScope ps(ctx, PH_J_METRIC);
     if (ctx->jmode == GBJK_J_CHOLESKY) {
       // h = L^-T (L^-1 g): no explicit V^-1
@@ -434,7 +449,7 @@ gbjk_status run_j(gbjk_ctx* ctx, const double* dP, double* dJ) {
     }
     k_j_colsum<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, naux * sizeof(double), ctx->stream>>>(
         ctx->d_B, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK, ctx->d_cmoff,
-        ctx->d_colmap, ctx->d_h, nbf, naux, dJ);
+        ctx->d_colmap, hvec, nbf, naux, dJ);
     CKL(PH_J_COLSUM);
   }
   return filter(ctx, dJ);
@@ -452,8 +467,9 @@ gbjk_status run_k(gbjk_ctx* ctx, int kmethod, const double* dC, int nocc, double
     CKL(PH_GATHER);
   }
   if ((s = launch_gemm(ctx, ctx->ht_tile0, ctx->ht_ntiles, false, 1.0, PH_HT))) return s;
-  const bool mo = kmethod == GBJK_K_DFMO;
-  if ((s = launch_gemm(ctx, mo ? ctx->fit_tile0 : ctx->fitV_tile0, ctx->fit_ntiles, false, 1.0,
+  const bool mo = kmethod == GBJK_K_DFMO || ctx->fitted;
+  if (!ctx->fitted &&
+      (s = launch_gemm(ctx, mo ? ctx->fit_tile0 : ctx->fitV_tile0, ctx->fit_ntiles, false, 1.0,
                        PH_FIT)))
     return s;
   if ((s = launch_gemm(ctx, mo ? ctx->syrk_tile0 : ctx->lmo_tile0,
@@ -629,6 +645,48 @@ gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices) {
   return GBJK_OK;
 }
 
+gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  ctx->fitted = fitted != 0;
+  ctx->split.fitted = ctx->fitted;
+  ctx->split.invalidate_b();
+  ctx->ws_nocc = -1;  // exchange plan reads H or the fitted H
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows) {
+  if (!ctx || rows < 0) return GBJK_INVALID_ARG;
+  ctx->split.xb_req = rows;
+  ctx->split.invalidate_b();
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, double decay) {
+  if (!ctx || !(decay > 0)) return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_synthetic: decay");
+  CK(cudaSetDevice(ctx->device));
+  gbjk_status s;
+  if ((s = dalloc(ctx, &ctx->d_B, (size_t)ctx->nnz))) return s;
+  {
+    PhaseScope ps(ctx, PH_GATHER);
+    k_synthetic_panels<<<dim3(cdiv(ctx->maxK, 128), ctx->naux, ctx->nbf), 128, 0, ctx->stream>>>(
+        ctx->d_B, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK, ctx->d_cmoff,
+        ctx->d_colmap, ctx->nbf, ctx->naux, seed, (float)decay);
+    CKL(PH_GATHER);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_B = true;
+  ctx->ws_nocc = -1;
+  ctx->split.invalidate_b();
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_download_b(gbjk_ctx* ctx, double* B) {
+  if (!ctx || !B || !ctx->have_B) return fail(ctx, GBJK_INVALID_ARG, "gbjk_download_b");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpy(B, ctx->d_B, (size_t)ctx->nnz * sizeof(double), cudaMemcpyDeviceToHost));
+  return GBJK_OK;
+}
+
 gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode) {
   if (!ctx) return GBJK_INVALID_ARG;
   if (jmode != GBJK_J_VINV && jmode != GBJK_J_CHOLESKY)
@@ -639,7 +697,7 @@ gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode) {
 
 static gbjk_status check_ready(gbjk_ctx* ctx) {
   if (!ctx) return GBJK_INVALID_ARG;
-  if (!ctx->have_B || !ctx->have_metric)
+  if (!ctx->have_B || (!ctx->have_metric && !ctx->fitted))
     return fail(ctx, GBJK_NOT_READY, "3-center tensor and metric must be uploaded first");
   if (cudaSetDevice(ctx->device) != cudaSuccess)
     return fail(ctx, GBJK_CUDA_ERROR, "cudaSetDevice failed");
@@ -679,6 +737,7 @@ static gbjk_status run_jk_split(gbjk_ctx* ctx, const double* dP, const double* d
   if ((s = ctx->split.run_k(ctx->stream, dK, &ctx->launches, &ctx->err))) return s;
   if ((s = filter(ctx, dK))) return s;
   if (!dJ) return GBJK_OK;
+  if (!ctx->split.fused_j()) return run_j(ctx, dP, dJ);  // auxiliary-batched: FP64 J
   CK(cudaMemsetAsync(dJ, 0, (size_t)nbf * nbf * sizeof(double), ctx->stream));
   {
     PhaseScope ps(ctx, PH_J_REDUCE);
@@ -712,9 +771,12 @@ gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, co
     return fail(ctx, GBJK_INVALID_ARG, "missing density or coefficients");
   if ((s = ensure_j_workspace(ctx))) return s;
   if (dK) {
+    if (ctx->precision == GBJK_SPLIT_BF16) {
+      if ((s = ensure_c_workspace(ctx, nocc))) return s;
+      if ((s = prepare_split(ctx, nocc))) return s;
+      return run_jk_split(ctx, dP, dC, nocc, dJ, dK);
+    }
     if ((s = ensure_k_workspace(ctx, nocc))) return s;
-    if ((s = prepare_split(ctx, nocc))) return s;
-    if (ctx->precision == GBJK_SPLIT_BF16) return run_jk_split(ctx, dP, dC, nocc, dJ, dK);
   }
   if (dJ && (s = run_j(ctx, dP, dJ))) return s;
   if (dK && (s = run_k(ctx, kmethod, dC, nocc, dK))) return s;
@@ -790,7 +852,7 @@ gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* P, const d
   const size_t n2 = (size_t)ctx->nbf * ctx->nbf;
   if (K) {
     if (!Cocc || nocc <= 0) return fail(ctx, GBJK_INVALID_ARG, "missing coefficients");
-    if ((s = ensure_k_workspace(ctx, nocc))) return s;
+    if ((s = ensure_c_workspace(ctx, nocc))) return s;
     CK(cudaMemcpyAsync(ctx->d_C, Cocc, (size_t)ctx->nbf * nocc * sizeof(double),
                        cudaMemcpyHostToDevice, ctx->stream));
   }

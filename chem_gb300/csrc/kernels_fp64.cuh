@@ -233,3 +233,60 @@ __global__ void k_block_filter(double* __restrict__ M, int n, const int* __restr
 }
 
 }  // namespace gbjk
+
+namespace gbjk {
+
+// Seeded synthetic 3-center tensor in the panel layout (the synthetic DF-K
+// workload): element (Y, mu, nu) = N(0,1)[seed, min(mu,nu), max(mu,nu), Y] *
+// exp(-0.5 |I - J| / decay), I and J the atom blocks of mu and nu, so the
+// tensor is symmetric in (mu, nu).  Normal deviates come from a splitmix64
+// hash of the indices through Box-Muller.  grid (ceil(maxK/128), naux, nbf).
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__global__ void k_synthetic_panels(double* __restrict__ B, const long long* __restrict__ panel_off,
+                                   const int* __restrict__ blk_of, const int* __restrict__ boff,
+                                   const int* __restrict__ panel_K, const int* __restrict__ cmoff,
+                                   const int* __restrict__ colmap, int nbf, int naux,
+                                   unsigned long long seed, float decay) {
+  const int mu = blockIdx.z;
+  const int Y = blockIdx.y;
+  const int I = blk_of[mu];
+  const int m = mu - boff[I];
+  const int KI = panel_K[I];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= KI) return;
+  const int nu = colmap[cmoff[I] + k];
+  const int J = blk_of[nu];
+  const unsigned long long a = (unsigned long long)min(mu, nu), b = (unsigned long long)max(mu, nu);
+  const unsigned long long h = splitmix64(seed ^ splitmix64((a * (unsigned long long)nbf + b) *
+                                                               (unsigned long long)naux + Y));
+  const float u1 = ((float)(h >> 40) + 0.5f) * (1.0f / 16777216.0f);
+  const float u2 = (float)((h >> 16) & 0xFFFFFF) * (1.0f / 16777216.0f);
+  const float g = sqrtf(-2.0f * logf(u1)) * cospif(2.0f * u2);
+  const float w = expf(-0.5f * fabsf((float)(I - J)) / decay);
+  B[panel_off[I] + ((long long)m * naux + Y) * KI + k] = (double)(g * w);
+}
+
+// out = alpha * sum_s part[s] (+ out when accumulate), upper triangle
+// mirrored when symmetric; order: existing value, then splits in order.
+__global__ void k_splitk_reduce_acc(const double* __restrict__ part, int nsplit, int n,
+                                    double alpha, int symmetric, int accumulate,
+                                    double* __restrict__ out) {
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= (long long)n * n) return;
+  const int m = (int)(idx / n), c = (int)(idx % n);
+  if (symmetric && c < m) return;
+  double s = 0.0;
+  for (int k = 0; k < nsplit; ++k) s += part[(long long)k * n * n + idx];
+  s *= alpha;
+  if (accumulate) s += out[idx];
+  out[idx] = s;
+  if (symmetric && c != m) out[(long long)c * n + m] = s;
+}
+
+}  // namespace gbjk

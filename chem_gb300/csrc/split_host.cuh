@@ -28,9 +28,17 @@ struct SplitState {
   std::vector<long long> panel_off;
   bool b_ready = false;
   int nocc = -1;
-  // A operands (static) and the prefitted tensor L^-1 B (FP64)
+  // A operands and the prefitted tensor L^-1 B (FP64).  With `fitted` the
+  // uploaded tensor already is L^-1 B and Bfit aliases it.
+  bool fitted = false;
+  bool bfit_owned = false;
   double* Bfit = nullptr;
   uint16_t* d_Aslices = nullptr;
+  // auxiliary batching: xb auxiliary rows per batch (nbatch > 1 streams the
+  // half transform and the exchange batch by batch; A digits per batch)
+  int xb_req = 0, xb = 0, nbatch = 1;
+  SplitJob* d_bjobs = nullptr;  // A-digit jobs, nbatch * nbf (one per (batch, mu))
+  int bjob_maxthr = 0;
   std::vector<long long> a_off, eA_off;
   std::vector<int> a_nrb, nkt;
   int* d_eA = nullptr;
@@ -100,12 +108,16 @@ struct SplitState {
     free_(&d_dt);
     free_(&d_items);
     free_(&d_jobs);
+    plans.clear();
     nocc = -1;
   }
   void release() {
     release_build();
-    free_(&Bfit);
+    if (bfit_owned) free_(&Bfit);
+    Bfit = nullptr;
+    bfit_owned = false;
     free_(&d_Aslices);
+    free_(&d_bjobs);
     free_(&d_eA);
     free_(&d_err);
     for (auto& pe : pending) {
@@ -195,67 +207,80 @@ struct SplitState {
   gbjk_status prepare_b(cudaStream_t st, const double* d_B, const double* d_Linv,
                         int64_t* launches, std::string* err) {
     const long long nnz = panel_off.back() + (long long)bsize.back() * naux * panelK.back();
-    double* d_Bfit = nullptr;
     if (alloc(&d_err, 1) != cudaSuccess || cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) {
       *err = "split path: cannot allocate the error flag";
       return GBJK_OOM;
     }
-    if (alloc(&d_Bfit, (size_t)nnz) != cudaSuccess) {
-      *err = "split path: out of memory for the prefitted tensor";
-      return GBJK_OOM;
-    }
-    // Bfit_I[m] = L^-1 B_I[m]  (naux x K_I per AO function m)
-    std::vector<GemmGroup> groups;
-    std::vector<GemmTile> tiles;
-    for (int I = 0; I < nblk; ++I) {
-      const int K = panelK[I];
-      if (K == 0) continue;
-      for (int m = 0; m < bsize[I]; ++m) {
-        GemmGroup g;
-        const long long off = panel_off[I] + (long long)m * naux * K;
-        g.A = d_Linv;
-        g.B = d_B + off;
-        g.C = d_Bfit + off;
-        g.M = naux;
-        g.N = K;
-        g.K = naux;
-        g.lda = naux;
-        g.ldb = K;
-        g.ldc = K;
-        g.flags = kLowerA;
-        for (int mt = 0; mt < cdiv_(naux, 64); ++mt)
-          for (int nt = 0; nt < cdiv_(K, 64); ++nt)
-            tiles.push_back({(int)groups.size(), mt, nt, 0, naux, 0});
-        groups.push_back(g);
+    xb = (xb_req > 0 && xb_req < naux) ? xb_req : naux;
+    nbatch = (naux + xb - 1) / xb;
+    double* d_Bfit = nullptr;
+    if (fitted) {
+      d_Bfit = const_cast<double*>(d_B);
+      bfit_owned = false;
+    } else {
+      if (alloc(&d_Bfit, (size_t)nnz) != cudaSuccess) {
+        *err = "split path: out of memory for the prefitted tensor";
+        return GBJK_OOM;
       }
-    }
-    GemmGroup* dg = nullptr;
-    GemmTile* dt = nullptr;
-    if (alloc(&dg, groups.size()) != cudaSuccess || alloc(&dt, tiles.size()) != cudaSuccess) {
-      free_(&dg);
-      free_(&d_Bfit);
-      *err = "split path: out of memory for the prefit plan";
-      return GBJK_OOM;
-    }
-    cudaMemcpy(dg, groups.data(), groups.size() * sizeof(GemmGroup), cudaMemcpyHostToDevice);
-    cudaMemcpy(dt, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice);
-    {
-      Scope sc(this, 3, st);
-      // the grid limit is 2^31-1 blocks; launch in slices of 1M tiles
-      for (size_t t0 = 0; t0 < tiles.size(); t0 += (1u << 20)) {
-        const int n = (int)std::min<size_t>(1u << 20, tiles.size() - t0);
-        k_gemm_fp64<false><<<n, 256, 0, st>>>(dg, dt + t0, 1.0);
-        (*launches)++;
+      bfit_owned = true;
+      // Bfit_I[m] = L^-1 B_I[m]  (naux x K_I per AO function m)
+      std::vector<GemmGroup> groups;
+      std::vector<GemmTile> tiles;
+      for (int I = 0; I < nblk; ++I) {
+        const int K = panelK[I];
+        if (K == 0) continue;
+        for (int m = 0; m < bsize[I]; ++m) {
+          GemmGroup g;
+          const long long off = panel_off[I] + (long long)m * naux * K;
+          g.A = d_Linv;
+          g.B = d_B + off;
+          g.C = d_Bfit + off;
+          g.M = naux;
+          g.N = K;
+          g.K = naux;
+          g.lda = naux;
+          g.ldb = K;
+          g.ldc = K;
+          g.flags = kLowerA;
+          for (int mt = 0; mt < cdiv_(naux, 64); ++mt)
+            for (int nt = 0; nt < cdiv_(K, 64); ++nt)
+              tiles.push_back({(int)groups.size(), mt, nt, 0, naux, 0});
+          groups.push_back(g);
+        }
       }
+      GemmGroup* dg = nullptr;
+      GemmTile* dt = nullptr;
+      if (alloc(&dg, groups.size()) != cudaSuccess || alloc(&dt, tiles.size()) != cudaSuccess) {
+        free_(&dg);
+        free_(&d_Bfit);
+        *err = "split path: out of memory for the prefit plan";
+        return GBJK_OOM;
+      }
+      cudaMemcpy(dg, groups.data(), groups.size() * sizeof(GemmGroup), cudaMemcpyHostToDevice);
+      cudaMemcpy(dt, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice);
+      {
+        Scope sc(this, 3, st);
+        // the grid limit is 2^31-1 blocks; launch in slices of 1M tiles
+        for (size_t t0 = 0; t0 < tiles.size(); t0 += (1u << 20)) {
+          const int n = (int)std::min<size_t>(1u << 20, tiles.size() - t0);
+          k_gemm_fp64<false><<<n, 256, 0, st>>>(dg, dt + t0, 1.0);
+          (*launches)++;
+        }
+      }
+      cudaStreamSynchronize(st);
+      cudaFree(dg);
+      cudaFree(dt);
     }
-    // A operands: rows (m, Y) of panel I, columns k
+    Bfit = d_Bfit;  // the mixed-mode J contracts it in FP64
+    // A operands: rows (m, y) of panel I, y < xb (all auxiliary rows when
+    // not batched), columns k
     a_off.assign(nblk, 0);
     eA_off.assign(nblk, 0);
     a_nrb.assign(nblk, 0);
     nkt.assign(nblk, 0);
     long long atot = 0, etot = 0;
     for (int I = 0; I < nblk; ++I) {
-      const long long rows = (long long)bsize[I] * naux;
+      const long long rows = (long long)bsize[I] * xb;
       a_nrb[I] = cdiv_(rows, kTileM) * (kTileM / 32);
       nkt[I] = std::max(1, cdiv_(panelK[I], kTileK));
       a_off[I] = atot;
@@ -266,48 +291,73 @@ struct SplitState {
     if (alloc(&d_Aslices, (size_t)atot) != cudaSuccess || alloc(&d_eA, (size_t)etot) != cudaSuccess ||
         cudaMemsetAsync(d_Aslices, 0, (size_t)atot * 2, st) != cudaSuccess ||
         cudaMemsetAsync(d_eA, 0, (size_t)etot * 4, st) != cudaSuccess) {
-      free_(&dg);
-      free_(&dt);
-      free_(&d_Bfit);
       *err = "split path: out of memory for the operand digits";
       return GBJK_OOM;
     }
-    std::vector<SplitJob> jobs(nblk);
-    int maxrows = 0;
-    long long maxthr = 0;
-    for (int I = 0; I < nblk; ++I) {
-      SplitJob& j = jobs[I];
-      j.src = d_Bfit + panel_off[I];
-      j.rs = panelK[I];
-      j.cs = 1;
-      j.row0 = 0;
-      j.nrows = bsize[I] * naux;
-      j.ncols = panelK[I];
-      j.e = d_eA + eA_off[I];
-      j.e_biased = 0;
-      j.nrb = a_nrb[I];
-      j.nkt = nkt[I];
-      j.dst = d_Aslices + a_off[I];
-      maxrows = std::max(maxrows, j.nrows);
-      maxthr = std::max(maxthr, (long long)(j.nrows / 8 + 2) * j.nkt * 32);
-    }
-    SplitJob* dj = nullptr;
-    if (alloc(&dj, jobs.size()) != cudaSuccess) {
-      *err = "split path: out of memory";
-      return GBJK_OOM;
-    }
-    cudaMemcpy(dj, jobs.data(), jobs.size() * sizeof(SplitJob), cudaMemcpyHostToDevice);
-    {
-      Scope sc(this, 2, st);
-      k_row_maxexp<<<dim3(cdiv_((long long)maxrows * 32, 256), nblk), 256, 0, st>>>(dj);
-      k_split_tiles<<<dim3(cdiv_(maxthr, 256), nblk), 256, 0, st>>>(dj);
-      *launches += 2;
+    if (nbatch == 1) {
+      std::vector<SplitJob> jobs(nblk);
+      int maxrows = 0;
+      long long maxthr = 0;
+      for (int I = 0; I < nblk; ++I) {
+        SplitJob& j = jobs[I];
+        j.src = d_Bfit + panel_off[I];
+        j.rs = panelK[I];
+        j.cs = 1;
+        j.row0 = 0;
+        j.nrows = bsize[I] * naux;
+        j.ncols = panelK[I];
+        j.e = d_eA + eA_off[I];
+        j.e_biased = 0;
+        j.nrb = a_nrb[I];
+        j.nkt = nkt[I];
+        j.dst = d_Aslices + a_off[I];
+        maxrows = std::max(maxrows, j.nrows);
+        maxthr = std::max(maxthr, (long long)(j.nrows / 8 + 2) * j.nkt * 32);
+      }
+      SplitJob* dj = nullptr;
+      if (alloc(&dj, jobs.size()) != cudaSuccess) {
+        *err = "split path: out of memory";
+        return GBJK_OOM;
+      }
+      cudaMemcpy(dj, jobs.data(), jobs.size() * sizeof(SplitJob), cudaMemcpyHostToDevice);
+      {
+        Scope sc(this, 2, st);
+        k_row_maxexp<<<dim3(cdiv_((long long)maxrows * 32, 256), nblk), 256, 0, st>>>(dj);
+        k_split_tiles<<<dim3(cdiv_(maxthr, 256), nblk), 256, 0, st>>>(dj);
+        *launches += 2;
+      }
+      cudaStreamSynchronize(st);
+      cudaFree(dj);
+    } else {
+      // one job per (batch, AO function): rows (m, y) of its panel
+      std::vector<SplitJob> jobs((size_t)nbatch * nbf);
+      bjob_maxthr = 0;
+      for (int b = 0; b < nbatch; ++b) {
+        const int Y0 = b * xb, xbc = std::min(xb, naux - Y0);
+        for (int I = 0; I < nblk; ++I)
+          for (int m = 0; m < bsize[I]; ++m) {
+            SplitJob& j = jobs[(size_t)b * nbf + boff[I] + m];
+            j.src = d_Bfit + panel_off[I] + ((long long)m * naux + Y0) * panelK[I];
+            j.rs = panelK[I];
+            j.cs = 1;
+            j.row0 = m * xbc;
+            j.nrows = xbc;
+            j.ncols = panelK[I];
+            j.e = d_eA + eA_off[I];
+            j.e_biased = 0;
+            j.nrb = a_nrb[I];
+            j.nkt = nkt[I];
+            j.dst = d_Aslices + a_off[I];
+            bjob_maxthr = std::max(bjob_maxthr, (xbc / 8 + 2) * nkt[I] * 32);
+          }
+      }
+      if (alloc(&d_bjobs, jobs.size()) != cudaSuccess) {
+        *err = "split path: out of memory for the batch jobs";
+        return GBJK_OOM;
+      }
+      cudaMemcpy(d_bjobs, jobs.data(), jobs.size() * sizeof(SplitJob), cudaMemcpyHostToDevice);
     }
     cudaError_t e = cudaStreamSynchronize(st);
-    cudaFree(dj);
-    cudaFree(dg);
-    cudaFree(dt);
-    Bfit = d_Bfit;  // kept: the mixed-mode J contracts it in FP64
     if (e != cudaSuccess) {
       *err = std::string("split path preparation: ") + cudaGetErrorString(e);
       return GBJK_CUDA_ERROR;
@@ -317,12 +367,37 @@ struct SplitState {
   }
 
   // --- per nocc: buffers and work lists ------------------------------------
+  // One plan per distinct auxiliary batch size (the last batch may be
+  // shorter): item ranges of the half transform and of the exchange.
+  struct BatchPlan {
+    int xbc, ht0, nht, k0, nk, ksplit, hjob;
+  };
+  std::vector<BatchPlan> plans;
+
+  int choose_ksplit(int nkt_total, int ntile) const {
+    const int ks_min = cdiv_(nkt_total, 256);  // int64 headroom: <= 8192 k per item
+    double best = 1e300;
+    int pick = ks_min;
+    for (int ks = ks_min; ks <= std::max(ks_min, 4 * nsm); ++ks) {
+      const int per = cdiv_(nkt_total, ks);
+      if (per < 8 && ks > ks_min) break;
+      const long long waves = ((long long)ntile * ks + nsm - 1) / nsm;
+      const double t = (double)waves * (per + 2.0);  // +2: per-item overhead in k-tiles
+      if (t < best) {
+        best = t;
+        pick = ks;
+      }
+    }
+    return pick;
+  }
+
   gbjk_status prepare_nocc(cudaStream_t st, int nocc_, std::string* err) {
     release_build();
+    const bool jfused = nbatch == 1;  // density rows ride along only unbatched
     maxb = 0;
     for (int I = 0; I < nblk; ++I) maxb = std::max(maxb, bsize[I]);
     // B operand rows of panel I: nocc orbitals, then b_I density rows
-    const int ntn = cdiv_(nocc_ + maxb, kTileN);
+    const int ntn = cdiv_(nocc_ + (jfused ? maxb : 0), kTileN);
     c_nrb = ntn * (kTileN / 32);
     c_off.assign(nblk, 0);
     long long ctot = 0;
@@ -331,12 +406,9 @@ struct SplitState {
       ctot += (long long)c_nrb * nkt[I] * kSlices * kImage;
     }
     hld = nocc_ + (nocc_ & 1);  // even row stride: 16-byte aligned pairs
-    const long long hk = (long long)naux * hld;
+    const long long hk = (long long)xb * hld;
     h_nkt = cdiv_(hk, kTileK);
     h_nrb = std::max(cdiv_(nbf, kTileM) * (kTileM / 32), cdiv_(nbf, kTileN) * (kTileN / 32));
-    // split-K of the exchange: items of at most 256 k-tiles (8192 k, the
-    // int64 headroom of the exact accumulator), count chosen to fill whole
-    // waves of persistent CTAs (one CTA per SM)
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -344,30 +416,18 @@ struct SplitState {
     for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
       for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt)
         if ((nt + 1) * kTileN > mt * kTileM) ++ntile;
-    {
-      const int ks_min = cdiv_(h_nkt, 256);
-      double best = 1e300;
-      ksplit = ks_min;
-      for (int ks = ks_min; ks <= std::max(ks_min, 4 * nsm); ++ks) {
-        const int per = cdiv_(h_nkt, ks);
-        if (per < 8 && ks > ks_min) break;
-        const long long waves = ((long long)ntile * ks + nsm - 1) / nsm;
-        const double t = (double)waves * (per + 2.0);  // +2: per-item overhead in k-tiles
-        if (t < best) {
-          best = t;
-          ksplit = ks;
-        }
-      }
-    }
-    const int kt_per = cdiv_(h_nkt, ksplit);
-    ksplit = cdiv_(h_nkt, kt_per);
+    std::vector<int> sizes = {xb};
+    const int xlast = naux - (nbatch - 1) * xb;
+    if (xlast != xb) sizes.push_back(xlast);
+    ksplit = 1;
+    for (int xbc : sizes) ksplit = std::max(ksplit, choose_ksplit(cdiv_((long long)xbc * hld, kTileK), ntile));
     if (alloc(&d_Cslices, (size_t)ctot) != cudaSuccess ||
         alloc(&d_eC, (size_t)nblk * c_nrb * 32) != cudaSuccess ||
         alloc(&d_H, (size_t)nbf * hk) != cudaSuccess ||
         alloc(&d_Hslices, (size_t)h_nrb * h_nkt * kSlices * kImage) != cudaSuccess ||
         alloc(&d_eH, (size_t)h_nrb * 32) != cudaSuccess ||
         alloc(&d_Kpart, (size_t)ksplit * nbf * nbf) != cudaSuccess ||
-        alloc(&d_dpart, (size_t)nbf * naux) != cudaSuccess ||
+        alloc(&d_dpart, jfused ? (size_t)nbf * naux : 1) != cudaSuccess ||
         alloc(&d_dt, (size_t)naux) != cudaSuccess ||
         cudaMemsetAsync(d_Cslices, 0, (size_t)ctot * 2, st) != cudaSuccess ||
         cudaMemsetAsync(d_eC, 0, (size_t)nblk * c_nrb * 32 * 4, st) != cudaSuccess ||
@@ -379,83 +439,113 @@ struct SplitState {
       return GBJK_OOM;
     }
     std::vector<SplitItem> items;
-    // half transform: Hfit rows (m, Y) of panel I, columns i
-    for (int I = 0; I < nblk; ++I) {
-      const long long rows = (long long)bsize[I] * naux;
-      const int ncolI = nocc_ + bsize[I];
-      for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
-        for (int nt = 0; nt < cdiv_(ncolI, kTileN); ++nt) {
-          SplitItem w;
-          w.a = d_Aslices + a_off[I];
-          w.a_nrb = a_nrb[I];
-          w.a_rb0 = mt * (kTileM / 32);
-          w.b = d_Cslices + c_off[I];
-          w.b_nrb = c_nrb;
-          w.b_rb0 = nt * (kTileN / 32);
-          w.kt0 = 0;
-          w.nkt = nkt[I];
-          w.ea = d_eA + eA_off[I] + (long long)mt * kTileM;
-          w.eb = d_eC + (long long)I * c_nrb * 32 + (long long)nt * kTileN;
-          w.out = d_H + ((long long)boff[I] * naux + (long long)mt * kTileM) * hld +
-                  (long long)nt * kTileN;
-          w.ldr = hld;
-          w.m_valid = (int)std::min<long long>(kTileM, rows - (long long)mt * kTileM);
-          w.n_valid = std::min(kTileN, ncolI - nt * kTileN);
-          // row (m, Y) of panel I belongs to H row mu = boff[I] + m
-          w.emax = (unsigned int*)d_eH + boff[I];
-          w.emax_row0 = mt * kTileM;
-          w.emax_div = naux;
-          // density column m' = col - nocc: g-partial of row (m, Y) if m' == m
-          w.out2 = d_dpart + (long long)boff[I] * naux;
-          w.c0 = nt * kTileN;
-          w.ncol1 = nocc_;
-          items.push_back(w);
-        }
+    std::vector<SplitJob> jobs(2 * nblk);
+    plans.clear();
+    for (size_t pi = 0; pi < sizes.size(); ++pi) {
+      const int xbc = sizes[pi];
+      BatchPlan pl;
+      pl.xbc = xbc;
+      // half transform: Hfit rows (m, y) of panel I, columns i (+ density)
+      pl.ht0 = (int)items.size();
+      for (int I = 0; I < nblk; ++I) {
+        const long long rows = (long long)bsize[I] * xbc;
+        const int ncolI = nocc_ + (jfused ? bsize[I] : 0);
+        for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
+          for (int nt = 0; nt < cdiv_(ncolI, kTileN); ++nt) {
+            SplitItem w;
+            w.a = d_Aslices + a_off[I];
+            w.a_nrb = a_nrb[I];
+            w.a_rb0 = mt * (kTileM / 32);
+            w.b = d_Cslices + c_off[I];
+            w.b_nrb = c_nrb;
+            w.b_rb0 = nt * (kTileN / 32);
+            w.kt0 = 0;
+            w.nkt = nkt[I];
+            w.ea = d_eA + eA_off[I] + (long long)mt * kTileM;
+            w.eb = d_eC + (long long)I * c_nrb * 32 + (long long)nt * kTileN;
+            w.out = d_H + ((long long)boff[I] * xbc + (long long)mt * kTileM) * hld +
+                    (long long)nt * kTileN;
+            w.ldr = hld;
+            w.m_valid = (int)std::min<long long>(kTileM, rows - (long long)mt * kTileM);
+            w.n_valid = std::min(kTileN, ncolI - nt * kTileN);
+            // row (m, y) of panel I belongs to H row mu = boff[I] + m
+            w.emax = (unsigned int*)d_eH + boff[I];
+            w.emax_row0 = mt * kTileM;
+            w.emax_div = xbc;
+            // density column m' = col - nocc: g-partial of row (m, Y) if m' == m
+            w.out2 = jfused ? d_dpart + (long long)boff[I] * naux : nullptr;
+            w.c0 = nt * kTileN;
+            w.ncol1 = nocc_;
+            items.push_back(w);
+          }
+      }
+      pl.nht = (int)items.size() - pl.ht0;
+      // exchange: upper tiles, split over k
+      const int nk_b = cdiv_((long long)xbc * hld, kTileK);
+      const int ksb = choose_ksplit(nk_b, ntile);
+      const int kt_per = cdiv_(nk_b, ksb);
+      pl.ksplit = cdiv_(nk_b, kt_per);
+      pl.k0 = (int)items.size();
+      for (int ks = 0; ks < pl.ksplit; ++ks) {
+        const int kt0 = ks * kt_per;
+        const int n_kt = std::min(kt_per, nk_b - kt0);
+        for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
+          for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt) {
+            if ((nt + 1) * kTileN <= mt * kTileM) continue;  // strictly below the diagonal
+            SplitItem w;
+            w.a = d_Hslices;
+            w.a_nrb = h_nrb;
+            w.a_rb0 = mt * (kTileM / 32);
+            w.b = d_Hslices;
+            w.b_nrb = h_nrb;
+            w.b_rb0 = nt * (kTileN / 32);
+            w.kt0 = kt0;
+            w.nkt = n_kt;
+            w.ea = d_eH + (long long)mt * kTileM;
+            w.eb = d_eH + (long long)nt * kTileN;
+            w.out = d_Kpart + (long long)ks * nbf * nbf + (long long)mt * kTileM * nbf +
+                    (long long)nt * kTileN;
+            w.ldr = nbf;
+            w.m_valid = std::min(kTileM, nbf - mt * kTileM);
+            w.n_valid = std::min(kTileN, nbf - nt * kTileN);
+            w.emax = nullptr;
+            w.emax_row0 = 0;
+            w.emax_div = 1;
+            w.out2 = nullptr;
+            w.c0 = 0;
+            w.ncol1 = 1 << 30;
+            items.push_back(w);
+          }
+      }
+      pl.nk = (int)items.size() - pl.k0;
+      // digits of the half-transformed batch (exponents from the epilogue)
+      SplitJob hj;
+      hj.src = d_H;
+      hj.rs = (long long)xbc * hld;
+      hj.cs = 1;
+      hj.row0 = 0;
+      hj.nrows = nbf;
+      hj.ncols = (long long)xbc * hld;
+      hj.e = d_eH;
+      hj.e_biased = 0;
+      hj.nrb = h_nrb;
+      hj.nkt = nk_b;
+      hj.dst = d_Hslices;
+      pl.hjob = (int)jobs.size();
+      jobs.push_back(hj);
+      plans.push_back(pl);
     }
-    ht_nitems = (int)items.size();
-    // exchange: upper tiles, split over k
-    for (int ks = 0; ks < ksplit; ++ks) {
-      const int kt0 = ks * kt_per;
-      const int n_kt = std::min(kt_per, h_nkt - kt0);
-      for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
-        for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt) {
-          if ((nt + 1) * kTileN <= mt * kTileM) continue;  // strictly below the diagonal
-          SplitItem w;
-          w.a = d_Hslices;
-          w.a_nrb = h_nrb;
-          w.a_rb0 = mt * (kTileM / 32);
-          w.b = d_Hslices;
-          w.b_nrb = h_nrb;
-          w.b_rb0 = nt * (kTileN / 32);
-          w.kt0 = kt0;
-          w.nkt = n_kt;
-          w.ea = d_eH + (long long)mt * kTileM;
-          w.eb = d_eH + (long long)nt * kTileN;
-          w.out = d_Kpart + (long long)ks * nbf * nbf + (long long)mt * kTileM * nbf +
-                  (long long)nt * kTileN;
-          w.ldr = nbf;
-          w.m_valid = std::min(kTileM, nbf - mt * kTileM);
-          w.n_valid = std::min(kTileN, nbf - nt * kTileN);
-          w.emax = nullptr;
-          w.emax_row0 = 0;
-          w.emax_div = 1;
-          w.out2 = nullptr;
-          w.c0 = 0;
-          w.ncol1 = 1 << 30;
-          items.push_back(w);
-        }
-    }
-    k_nitems = (int)items.size() - ht_nitems;
-    std::vector<SplitJob> jobs(2 * nblk + 1);
+    ht_nitems = plans[0].nht;
+    k_nitems = plans[0].nk;
     c_maxthreads = 0;
     c_maxrows = std::max(nocc_, maxb);
     for (int I = 0; I < nblk; ++I) {
-      SplitJob& pj = jobs[nblk + I];  // density rows: Pg panel rows
+      SplitJob& pj = jobs[nblk + I];  // density rows: Pg panel rows (none when batched)
       pj.src = nullptr;               // set per build
       pj.rs = panelK[I];
       pj.cs = 1;
       pj.row0 = nocc_;
-      pj.nrows = bsize[I];
+      pj.nrows = jfused ? bsize[I] : 0;
       pj.ncols = panelK[I];
       pj.e = d_eC + (long long)I * c_nrb * 32;
       pj.e_biased = 0;
@@ -476,19 +566,6 @@ struct SplitState {
       j.dst = d_Cslices + c_off[I];
       c_maxthreads = std::max(c_maxthreads, ((nocc_ + maxb) / 8 + 2) * nkt[I] * 32);
     }
-    SplitJob& hj = jobs[2 * nblk];
-    hj.src = d_H;
-    hj.rs = hk;
-    hj.cs = 1;
-    hj.row0 = 0;
-    hj.nrows = nbf;
-    hj.ncols = hk;
-    hj.e = d_eH;  // from the half-transform epilogue, unbiased before use
-    hj.e_biased = 0;
-    hj.nrb = h_nrb;
-    hj.nkt = h_nkt;
-    hj.dst = d_Hslices;
-    h_threads = (long long)(nbf / 8 + 2) * h_nkt * 32;
     if (alloc(&d_items, items.size()) != cudaSuccess || alloc(&d_jobs, jobs.size()) != cudaSuccess) {
       release_build();
       *err = "split path: out of memory for the work lists";
@@ -496,8 +573,8 @@ struct SplitState {
     }
     cudaMemcpy(d_items, items.data(), items.size() * sizeof(SplitItem), cudaMemcpyHostToDevice);
     host_jobs = jobs;
+    jobs_cg = jobs_pg = nullptr;
     nocc = nocc_;
-    (void)st;
     return GBJK_OK;
   }
   std::vector<SplitJob> host_jobs;
@@ -515,16 +592,18 @@ struct SplitState {
         host_jobs[I].src = d_Cg_ + (long long)cmoff[I] * nocc_;
         host_jobs[nblk + I].src = d_Pg + pg_off[I];
       }
+      jobs_cg = d_Cg_;
       jobs_pg = d_Pg;
       if (cudaMemcpy(d_jobs, host_jobs.data(), host_jobs.size() * sizeof(SplitJob),
                      cudaMemcpyHostToDevice) != cudaSuccess) {
         *err = "split path: job upload failed";
         return GBJK_CUDA_ERROR;
       }
-      jobs_cg = d_Cg_;
     }
     return GBJK_OK;
   }
+
+  bool fused_j() const { return nbatch == 1; }
 
   // --- per build ------------------------------------------------------------
   gbjk_status run_k(cudaStream_t st, double* dK, int64_t* launches, std::string* err) {
@@ -535,28 +614,39 @@ struct SplitState {
       k_split_tiles<<<dim3(cdiv_((long long)c_maxthreads, 256), 2 * nblk), 256, 0, st>>>(d_jobs);
       *launches += 2;
     }
-    {
-      Scope sc(this, 0, st);
-      // H row exponents are atomically maximised by the half-transform epilogue
-      if (cudaMemsetAsync(d_eH, 0, (size_t)h_nrb * 32 * sizeof(int), st) != cudaSuccess) {
-        *err = "split path: memset failed";
-        return GBJK_CUDA_ERROR;
+    for (int b = 0; b < nbatch; ++b) {
+      const BatchPlan& pl = plans[(b == nbatch - 1 && plans.size() > 1) ? 1 : 0];
+      if (nbatch > 1) {
+        Scope sc(this, 2, st);
+        const SplitJob* bj = d_bjobs + (size_t)b * nbf;
+        k_row_maxexp<<<dim3(cdiv_((long long)pl.xbc * 32, 256), nbf), 256, 0, st>>>(bj);
+        k_split_tiles<<<dim3(cdiv_((long long)bjob_maxthr, 256), nbf), 256, 0, st>>>(bj);
+        *launches += 2;
       }
-      if ((s = launch_gemm(st, d_items, ht_nitems, launches, err))) return s;
+      {
+        Scope sc(this, 0, st);
+        // H row exponents are atomically maximised by the half-transform epilogue
+        if (cudaMemsetAsync(d_eH, 0, (size_t)h_nrb * 32 * sizeof(int), st) != cudaSuccess) {
+          *err = "split path: memset failed";
+          return GBJK_CUDA_ERROR;
+        }
+        if ((s = launch_gemm(st, d_items + pl.ht0, pl.nht, launches, err))) return s;
+      }
+      {
+        Scope sc(this, 2, st);
+        k_exp_unbias<<<cdiv_((long long)h_nrb * 32, 256), 256, 0, st>>>(d_eH, h_nrb * 32);
+        const long long hthr = (long long)(nbf / 8 + 2) * cdiv_((long long)pl.xbc * hld, kTileK) * 32;
+        k_split_tiles<<<dim3(cdiv_(hthr, 256), 1), 256, 0, st>>>(d_jobs + pl.hjob);
+        *launches += 2;
+      }
+      {
+        Scope sc(this, 1, st);
+        if ((s = launch_gemm(st, d_items + pl.k0, pl.nk, launches, err))) return s;
+      }
+      k_splitk_reduce_acc<<<cdiv_((long long)nbf * nbf, 256), 256, 0, st>>>(
+          d_Kpart, pl.ksplit, nbf, -1.0, 1, b > 0 ? 1 : 0, dK);
+      (*launches)++;
     }
-    {
-      Scope sc(this, 2, st);
-      k_exp_unbias<<<cdiv_((long long)h_nrb * 32, 256), 256, 0, st>>>(d_eH, h_nrb * 32);
-      k_split_tiles<<<dim3(cdiv_(h_threads, 256), 1), 256, 0, st>>>(d_jobs + 2 * nblk);
-      *launches += 2;
-    }
-    {
-      Scope sc(this, 1, st);
-      if ((s = launch_gemm(st, d_items + ht_nitems, k_nitems, launches, err))) return s;
-    }
-    k_splitk_reduce<<<cdiv_((long long)nbf * nbf, 256), 256, 0, st>>>(d_Kpart, ksplit, nbf, -1.0,
-                                                                      1, dK);
-    (*launches)++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       *err = std::string("split path launch: ") + cudaGetErrorString(e);

@@ -57,6 +57,10 @@ def lib():
         L.gbjk_upload_metric.argtypes = [vp, dp, dp]
         L.gbjk_set_precision.argtypes = [vp, C.c_int, C.c_int]
         L.gbjk_set_jmode.argtypes = [vp, C.c_int]
+        L.gbjk_set_fitted.argtypes = [vp, C.c_int]
+        L.gbjk_set_aux_batch.argtypes = [vp, C.c_int]
+        L.gbjk_upload_b_synthetic.argtypes = [vp, C.c_ulonglong, C.c_double]
+        L.gbjk_download_b.argtypes = [vp, dp]
         L.gbjk_compute_j.argtypes = [vp, dp, dp]
         L.gbjk_compute_k.argtypes = [vp, C.c_int, dp, C.c_int, dp]
         L.gbjk_compute_jk.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, dp]
@@ -98,7 +102,10 @@ class JKEngine:
     """One gbjk context: the resident 3-center tensor and metric of a molecule."""
 
     def __init__(self, layout, B, Linv, Vinv, eps=0.0, device=0, precision=GBJK_FP64,
-                 nslices=0):
+                 nslices=0, fitted=False, synthetic=None, aux_batch=0):
+        """B: host panel array, or None with synthetic=(seed, decay) to
+        generate it on the device.  fitted: B already is L^-1 B (Linv and
+        Vinv may be None).  aux_batch: split path auxiliary batch rows."""
         L = lib()
         self.layout = layout
         self.nbf, self.naux = layout.nbf, layout.naux
@@ -115,13 +122,25 @@ class JKEngine:
         if rc != 0:
             raise RuntimeError(f"gbjk_create failed: {STATUS.get(rc, rc)}")
         self.h = h
-        B = np.ascontiguousarray(B, float)
-        if B.size != layout.nnz:
-            raise ValueError("B does not match the layout")
-        self._check(L.gbjk_upload_b(h, _dp(B)), "gbjk_upload_b")
-        self._check(L.gbjk_upload_metric(h, _dp(np.ascontiguousarray(Linv, float)),
-                                         _dp(np.ascontiguousarray(Vinv, float))),
-                    "gbjk_upload_metric")
+        if fitted:
+            self._check(L.gbjk_set_fitted(h, 1), "gbjk_set_fitted")
+        if aux_batch:
+            self._check(L.gbjk_set_aux_batch(h, int(aux_batch)), "gbjk_set_aux_batch")
+        if B is None:
+            if synthetic is None:
+                raise ValueError("B or synthetic=(seed, decay) is required")
+            seed, decay = synthetic
+            self._check(L.gbjk_upload_b_synthetic(h, int(seed), float(decay)),
+                        "gbjk_upload_b_synthetic")
+        else:
+            B = np.ascontiguousarray(B, float)
+            if B.size != layout.nnz:
+                raise ValueError("B does not match the layout")
+            self._check(L.gbjk_upload_b(h, _dp(B)), "gbjk_upload_b")
+        if Linv is not None:
+            self._check(L.gbjk_upload_metric(h, _dp(np.ascontiguousarray(Linv, float)),
+                                             _dp(np.ascontiguousarray(Vinv, float))),
+                        "gbjk_upload_metric")
         self.set_precision(precision, nslices)
 
     def _check(self, rc, what):
@@ -136,6 +155,11 @@ class JKEngine:
         self._check(lib().gbjk_set_precision(self.h, int(precision), int(nslices)),
                     "gbjk_set_precision")
         self.precision = precision
+
+    def download_b(self):
+        B = np.empty(self.layout.nnz)
+        self._check(lib().gbjk_download_b(self.h, _dp(B)), "gbjk_download_b")
+        return B
 
     def set_jmode(self, jmode):
         """'vinv' (reference route, default) or 'cholesky'."""

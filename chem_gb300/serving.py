@@ -78,10 +78,14 @@ class _Resident:
 class FockServer:
     """Serves Request objects; see the module docstring."""
 
-    def __init__(self, budget_bytes=150e9, slots=8, precision="split", device=0,
-                 engine_factory=None, clock=time.perf_counter, drop_host_tensor=True):
+    def __init__(self, budget_bytes=150e9, slots=4, precision="split", device=0,
+                 engine_factory=None, clock=time.perf_counter, drop_host_tensor=True,
+                 max_host_bytes=48e9):
         self.budget = int(budget_bytes)
         self.drop_host_tensor = drop_host_tensor
+        self.max_host_bytes = int(max_host_bytes)
+        self._host_pending = 0
+        self._host_bytes = {}
         self.slots = slots
         self.precision = precision
         self.device = device
@@ -141,9 +145,15 @@ class FockServer:
             # the molecule up again (only after an eviction)
             self._systems[req.key] = req.make_system()
             ds = self._systems[req.key][0]
+            with self._cv:
+                self._host_bytes[req.key] = int(ds.B.nbytes)
+                self._host_pending += int(ds.B.nbytes)
         eng = self._engine_factory(ds)
-        if self.drop_host_tensor and hasattr(ds, "B"):
+        if self.drop_host_tensor and getattr(ds, "B", None) is not None:
             ds.B = None  # the engine holds the device copy
+            with self._cv:
+                self._host_pending -= self._host_bytes.pop(req.key, 0)
+                self._cv.notify_all()
         r = _Resident(eng, need)
         r.busy = 1
         with self._cv:
@@ -173,8 +183,18 @@ class FockServer:
 
     # -- request flow ----------------------------------------------------------
     def _setup(self, req):
+        # back-pressure: the set-up pipeline pauses while the host tensors of
+        # molecules set up but not yet resident exceed max_host_bytes
+        with self._cv:
+            while self._host_pending > self.max_host_bytes:
+                self._cv.wait(0.1)
         if req.key not in self._systems:
-            self._systems[req.key] = req.make_system()
+            sysm = req.make_system()
+            nb = int(getattr(getattr(sysm[0], "B", None), "nbytes", 0) or 0)
+            with self._cv:
+                self._systems[req.key] = sysm
+                self._host_pending += nb
+                self._host_bytes[req.key] = nb
 
     def _on_setup(self, req, t0):
         req.t_setup_done = self.clock() - t0

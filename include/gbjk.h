@@ -92,6 +92,23 @@ gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* 
  * operand for the split path (ignored for FP64; 0 picks the default). */
 gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices);
 
+/* fitted != 0: the uploaded tensor already is L^-1 (X|mu nu) (pre-fitted);
+ * no metric is used: J = B^T (B Ptot), K = -(B C)^T (B C).  Used by the
+ * synthetic DF-K workload, whose tensor is treated as pre-fitted.
+ * No counterpart in the reference. */
+gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted);
+/* Split path: process the auxiliary index in batches of `rows` (0 = all at
+ * once), streaming the half transform and the exchange batch by batch so
+ * that the half-transformed tensor never exists in full.  No counterpart in
+ * the reference (it batches over X with DBCSR, src/fock/jkdf.cpp:412-422). */
+gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows);
+/* Fill the panel array on the device with the seeded synthetic tensor
+ * (Y, mu, nu) = N(0,1)[seed, min(mu,nu), max(mu,nu), Y] exp(-|I-J|/(2 decay)),
+ * symmetric in (mu, nu); gbjk_download_b copies the panels to the host.
+ * No counterpart in the reference. */
+gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, double decay);
+gbjk_status gbjk_download_b(gbjk_ctx* ctx, double* B);
+
 /* jmode: GBJK_J_VINV (default, the reference route) or GBJK_J_CHOLESKY.
  * No counterpart in the reference. */
 gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode);

@@ -257,7 +257,8 @@ static void contract_k(const oracle_layout* L, const double* A, const double* Bm
 }
 
 /* DF-MO K: HT1 = B C, HT2 = L^-1 HT1, K = -HT2^T HT2  (jkdf.cpp:348-438).
- * Linv is the lower-triangular inverse Cholesky factor of the metric. */
+ * Linv is the lower-triangular inverse Cholesky factor of the metric, or
+ * NULL for a pre-fitted tensor (HT2 = HT1). */
 int oracle_dfmo_k(const oracle_layout* L, const double* B, const double* Linv, const double* Cm,
                   int nocc, double* K, double eps, long long kchunk) {
   const size_t sz = (size_t)L->nbf * L->naux * nocc;
@@ -265,7 +266,10 @@ int oracle_dfmo_k(const oracle_layout* L, const double* B, const double* Linv, c
   double* H2 = (double*)malloc(sizeof(double) * sz);
   if (!H || !H2) { free(H); free(H2); return 2; }
   oracle_half_transform(L, B, Cm, nocc, H);
-  apply_metric(L, Linv, 1, H, nocc, H2);
+  if (Linv)
+    apply_metric(L, Linv, 1, H, nocc, H2);
+  else  /* pre-fitted tensor: no metric */
+    memcpy(H2, H, sizeof(double) * sz);
   contract_k(L, H2, H2, nocc, K, 1, kchunk);
   oracle_filter(L, K, eps);
   free(H);

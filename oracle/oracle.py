@@ -105,7 +105,8 @@ class Oracle:
         n = self.layout.nbf
         K = np.zeros((n, n))
         Cocc = np.ascontiguousarray(Cocc, float)
-        rc = lib().oracle_dfmo_k(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Linv)),
+        lp = None if Linv is None else _dp(np.ascontiguousarray(Linv))
+        rc = lib().oracle_dfmo_k(C.byref(self.L), _dp(self.B), lp,
                                  _dp(Cocc), Cocc.shape[1], _dp(K), eps, int(kchunk))
         if rc:
             raise MemoryError("oracle_dfmo_k")
