@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "gbjk.h"
 #include "kernels_fp64.cuh"
+#include "mp2_host.cuh"
 #include "split_host.cuh"
 
 using namespace gbjk;
@@ -95,6 +96,8 @@ struct gbjk_ctx {
   int precision = GBJK_FP64;
   int nslices = 0;
   SplitState split;
+  // SOS-AO-MP2 Laplace batch (ll_full Z builder) on the prefitted tensor
+  Mp2State mp2;
   // profiling
   bool profile = false;
   cudaEvent_t ev[PH_COUNT][2] = {};
@@ -587,6 +590,7 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  ctx->mp2.release();
   ctx->split.release();
   void* ptrs[] = {ctx->d_blk_of, ctx->d_boff,  ctx->d_panelK, ctx->d_cmoff, ctx->d_colmap,
                   ctx->d_panel_off, ctx->d_pg_off, ctx->d_B, ctx->d_Linv, ctx->d_Vinv,
@@ -616,6 +620,7 @@ gbjk_status gbjk_upload_b(gbjk_ctx* ctx, const double* B) {
   CK(cudaMemcpy(ctx->d_B, B, (size_t)ctx->nnz * sizeof(double), cudaMemcpyHostToDevice));
   ctx->have_B = true;
   ctx->ws_nocc = -1;  // plans hold d_B
+  ctx->mp2.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -630,6 +635,7 @@ gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* 
   CK(cudaMemcpy(ctx->d_Vinv, Vinv, n2 * sizeof(double), cudaMemcpyHostToDevice));
   ctx->have_metric = true;
   ctx->ws_nocc = -1;
+  ctx->mp2.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -649,6 +655,7 @@ gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
   if (!ctx) return GBJK_INVALID_ARG;
   ctx->fitted = fitted != 0;
   ctx->split.fitted = ctx->fitted;
+  ctx->mp2.release();
   ctx->split.invalidate_b();
   ctx->ws_nocc = -1;  // exchange plan reads H or the fitted H
   return GBJK_OK;
@@ -657,6 +664,7 @@ gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
 gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows) {
   if (!ctx || rows < 0) return GBJK_INVALID_ARG;
   ctx->split.xb_req = rows;
+  ctx->mp2.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -676,6 +684,7 @@ gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, doub
   CK(cudaStreamSynchronize(ctx->stream));
   ctx->have_B = true;
   ctx->ws_nocc = -1;
+  ctx->mp2.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -878,7 +887,9 @@ gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int n
   return gbjk_compute_jk(ctx, kmethod, nullptr, Cocc, nocc, nullptr, K);
 }
 
-size_t gbjk_device_bytes(const gbjk_ctx* ctx) { return ctx ? ctx->dev_bytes + ctx->split.bytes : 0; }
+size_t gbjk_device_bytes(const gbjk_ctx* ctx) {
+  return ctx ? ctx->dev_bytes + ctx->split.bytes + ctx->mp2.bytes : 0;
+}
 int64_t gbjk_kernel_launches(const gbjk_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
 gbjk_status gbjk_profile(gbjk_ctx* ctx, int enable) {
@@ -887,6 +898,8 @@ gbjk_status gbjk_profile(gbjk_ctx* ctx, int enable) {
   resolve_profile(ctx);
   ctx->profile = enable != 0;
   ctx->split.profile = enable != 0;
+  ctx->mp2.profile = enable != 0;
+  ctx->mp2.reset_profile();
   for (int i = 0; i < PH_COUNT; ++i) {
     ctx->ph_ms[i] = 0;
     ctx->ph_launch[i] = 0;
@@ -904,7 +917,83 @@ int gbjk_profile_read(const gbjk_ctx* ctx, int idx, const char** name, double* m
     if (launches) *launches = ctx->ph_launch[idx];
     return 1;
   }
-  return const_cast<gbjk_ctx*>(ctx)->split.profile_read(idx - PH_COUNT, name, ms, launches);
+  gbjk_ctx* c = const_cast<gbjk_ctx*>(ctx);
+  if (c->split.profile_read(idx - PH_COUNT, name, ms, launches)) return 1;
+  return c->mp2.profile_read(idx - PH_COUNT - 4, name, ms, launches);
+}
+
+// --- SOS-AO-MP2 Laplace batch -----------------------------------------------
+
+gbjk_status gbjk_mp2_set_factors(gbjk_ctx* ctx, int npts, const int* rank_o,
+                                 const double* const* Lo, const int* rank_v,
+                                 const double* const* Lv) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (npts < 1 || !rank_o || !Lo || !rank_v || !Lv)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_mp2_set_factors: null argument or npts < 1");
+  for (int t = 0; t < npts; ++t) {
+    if (!Lo[t] || !Lv[t])
+      return fail(ctx, GBJK_INVALID_ARG, "gbjk_mp2_set_factors: null factor");
+    if (rank_o[t] < 1 || rank_o[t] > ctx->nbf || rank_v[t] < 1 || rank_v[t] > ctx->nbf)
+      return fail(ctx, GBJK_INVALID_ARG, "gbjk_mp2_set_factors: rank out of range [1, nbf]");
+  }
+  if (!ctx->split.b_ready &&
+      (s = ctx->split.prepare_b(ctx->stream, ctx->d_B, ctx->d_Linv, &ctx->launches, &ctx->err)))
+    return s;
+  Mp2State& m = ctx->mp2;
+  bool same = m.ready && m.precision == ctx->precision && m.npts == npts;
+  for (int t = 0; same && t < npts; ++t) same = m.ro[t] == rank_o[t] && m.rv[t] == rank_v[t];
+  if (!same && (s = m.plan(ctx->stream, ctx->precision, npts, rank_o, rank_v, ctx->nbf, ctx->naux,
+                           ctx->nblk, ctx->ncols_total, ctx->bsize, ctx->boff, ctx->panelK,
+                           ctx->cmoff, ctx->panel_off, ctx->split, &ctx->err)))
+    return s;
+  return m.upload(ctx->stream, ctx->nbf, Lo, Lv, &ctx->err);
+}
+
+gbjk_status gbjk_mp2_compute_dev(gbjk_ctx* ctx) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (!ctx->mp2.ready || ctx->mp2.precision != ctx->precision)
+    return fail(ctx, GBJK_NOT_READY, "gbjk_mp2_compute_dev: set the factors first (after any precision change)");
+  return ctx->mp2.run(ctx->stream, ctx->nbf, ctx->naux, ctx->nblk, ctx->ncols_total,
+                      ctx->d_colmap, ctx->split, &ctx->launches, &ctx->err);
+}
+
+gbjk_status gbjk_mp2_read(gbjk_ctx* ctx, double* energies, double* Z) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (!ctx->mp2.have_result) return fail(ctx, GBJK_NOT_READY, "gbjk_mp2_read: nothing computed");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->mp2.precision == GBJK_SPLIT_BF16) {
+    const int code = ctx->split.read_error();
+    if (code != 0)
+      return fail(ctx, GBJK_TIMEOUT,
+                  "split GEMM: a pipeline wait timed out (code " + std::to_string(code) + ")");
+  }
+  const int npts = ctx->mp2.npts;
+  if (energies)
+    CK(cudaMemcpy(energies, ctx->mp2.d_E, (size_t)npts * sizeof(double), cudaMemcpyDeviceToHost));
+  if (Z)
+    CK(cudaMemcpy(Z, ctx->mp2.d_Z, (size_t)npts * ctx->naux * ctx->naux * sizeof(double),
+                  cudaMemcpyDeviceToHost));
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_mp2_laplace(gbjk_ctx* ctx, int npts, const int* rank_o, const double* const* Lo,
+                             const int* rank_v, const double* const* Lv, double* energies,
+                             double* Z) {
+  gbjk_status s;
+  if ((s = gbjk_mp2_set_factors(ctx, npts, rank_o, Lo, rank_v, Lv))) return s;
+  if ((s = gbjk_mp2_compute_dev(ctx))) return s;
+  return gbjk_mp2_read(ctx, energies, Z);
+}
+
+gbjk_status gbjk_mp2_release(gbjk_ctx* ctx) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->mp2.release();
+  return GBJK_OK;
 }
 
 }  // extern "C"

@@ -123,7 +123,8 @@ __global__ void k_j_colsum(const double* __restrict__ B, const long long* __rest
 }
 
 // Grouped FP64 GEMM over a tile list; 64x64 tiles, 256 threads, 4x4 per thread.
-template <bool TRANSB>
+// TRANSA: A is stored K x M row-major, op(A)(m, k) = A[k * lda + m].
+template <bool TRANSB, bool TRANSA = false>
 __global__ void __launch_bounds__(256)
     k_gemm_fp64(const GemmGroup* __restrict__ groups, const GemmTile* __restrict__ tiles,
                 double alpha) {
@@ -145,9 +146,15 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
       const int idx = tid + 256 * r;
-      const int row = idx >> 4, kk = idx & 15;
-      const int gm = m0 + row, gk = k0 + kk;
-      As[kk][row] = (gm < g.M && gk < kend) ? g.A[(long long)gm * g.lda + gk] : 0.0;
+      if (TRANSA) {
+        const int kk = idx >> 6, row = idx & 63;
+        const int gm = m0 + row, gk = k0 + kk;
+        As[kk][row] = (gm < g.M && gk < kend) ? g.A[(long long)gk * g.lda + gm] : 0.0;
+      } else {
+        const int row = idx >> 4, kk = idx & 15;
+        const int gm = m0 + row, gk = k0 + kk;
+        As[kk][row] = (gm < g.M && gk < kend) ? g.A[(long long)gm * g.lda + gk] : 0.0;
+      }
     }
 #pragma unroll
     for (int r = 0; r < 4; ++r) {

@@ -81,6 +81,12 @@ def lib():
         L.gbjk_profile.argtypes = [vp, C.c_int]
         L.gbjk_profile_read.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), dp,
                                         C.POINTER(C.c_int64)]
+        ip, dpp = C.POINTER(C.c_int), C.POINTER(dp)
+        L.gbjk_mp2_set_factors.argtypes = [vp, C.c_int, ip, dpp, ip, dpp]
+        L.gbjk_mp2_compute_dev.argtypes = [vp]
+        L.gbjk_mp2_read.argtypes = [vp, dp, dp]
+        L.gbjk_mp2_laplace.argtypes = [vp, C.c_int, ip, dpp, ip, dpp, dp, dp]
+        L.gbjk_mp2_release.argtypes = [vp]
         _lib = L
     return _lib
 
@@ -210,6 +216,47 @@ class JKEngine:
 
     def profile(self, enable=True):
         self._check(lib().gbjk_profile(self.h, int(enable)), "gbjk_profile")
+
+    # --- SOS-AO-MP2 Laplace batch (gbjk_mp2_*) ------------------------------
+    def mp2_set_factors(self, Lo, Lv):
+        """Lo, Lv: per Laplace point, the occupied (nbf x r_t) and virtual
+        (nbf x rv_t) Cholesky factors of the pseudo-densities."""
+        if len(Lo) != len(Lv) or not Lo:
+            raise ValueError("need one occupied and one virtual factor per point")
+        lo = [np.ascontiguousarray(a, float) for a in Lo]
+        lv = [np.ascontiguousarray(a, float) for a in Lv]
+        for a in lo + lv:
+            if a.ndim != 2 or a.shape[0] != self.nbf:
+                raise ValueError("factors must be nbf x rank")
+        n = len(lo)
+        ro = np.array([a.shape[1] for a in lo], np.int32)
+        rv = np.array([a.shape[1] for a in lv], np.int32)
+        dpp = C.POINTER(C.c_double) * n
+        plo, plv = dpp(*[_dp(a) for a in lo]), dpp(*[_dp(a) for a in lv])
+        self._check(lib().gbjk_mp2_set_factors(self.h, n, ro.ctypes.data_as(C.POINTER(C.c_int)), plo,
+                                               rv.ctypes.data_as(C.POINTER(C.c_int)), plv),
+                    "gbjk_mp2_set_factors")
+        self._mp2_npts = n
+
+    def mp2_compute_dev(self):
+        self._check(lib().gbjk_mp2_compute_dev(self.h), "gbjk_mp2_compute_dev")
+
+    def mp2_read(self, want_z=False):
+        """(e_t per point, Z~_t stacked or None)."""
+        n = self._mp2_npts
+        e = np.zeros(n)
+        Z = np.zeros((n, self.naux, self.naux)) if want_z else None
+        self._check(lib().gbjk_mp2_read(self.h, _dp(e), _dp(Z) if want_z else None),
+                    "gbjk_mp2_read")
+        return e, Z
+
+    def mp2_laplace(self, Lo, Lv, want_z=False):
+        self.mp2_set_factors(Lo, Lv)
+        self.mp2_compute_dev()
+        return self.mp2_read(want_z)
+
+    def mp2_release(self):
+        self._check(lib().gbjk_mp2_release(self.h), "gbjk_mp2_release")
 
     def profile_read(self):
         out = {}

@@ -8,8 +8,12 @@ workspaces) and serves requests as they arrive:
 * set-up — the host integrals of a molecule not seen before run on a CPU
   pipeline (one job at a time, each using all host threads);
 * admission — a molecule's engine is created when its device footprint fits
-  the HBM budget; idle engines are evicted least-recently-used to make room;
-  a request waits until its engine is resident and a GPU slot is free;
+  the HBM budget; idle engines are evicted to make room, first those with
+  no requests waiting (least-recently-used first), then any idle one;
+* scheduling — a free GPU slot takes the earliest waiting request whose
+  molecule is resident and idle, else the earliest request of a molecule
+  that is neither resident nor being admitted; so the requests of a
+  resident molecule are served together before it is evicted;
 * execution — GPU slots are host threads, each issuing builds on its own
   engine's CUDA stream, so builds of different molecules overlap on the
   device; a molecule's builds are serialised on its engine.
@@ -22,7 +26,7 @@ same boundary.
 """
 from __future__ import annotations
 
-import heapq
+import bisect
 import threading
 import time
 from collections import OrderedDict
@@ -80,10 +84,11 @@ class FockServer:
 
     def __init__(self, budget_bytes=150e9, slots=4, precision="split", device=0,
                  engine_factory=None, clock=time.perf_counter, drop_host_tensor=True,
-                 max_host_bytes=48e9):
+                 max_host_bytes=48e9, progress=None):
         self.budget = int(budget_bytes)
         self.drop_host_tensor = drop_host_tensor
         self.max_host_bytes = int(max_host_bytes)
+        self.progress = progress  # callable(done, total) after each request
         self._host_pending = 0
         self._host_bytes = {}
         self.slots = slots
@@ -96,7 +101,10 @@ class FockServer:
         self._used = 0
         self._systems = {}               # key -> (ds, P, C) once set up
         self._setup_pending = {}         # key -> future
-        self._ready = []                 # heap of (arrival, rid, request)
+        self._ready = []                 # sorted list of (arrival, rid, request)
+        self._waiting = {}               # key -> requests submitted, not yet taken
+        self._admitting = set()          # keys whose engine a slot is creating
+        self._taken = 0
         self._cpu = ThreadPoolExecutor(1)
         self.max_used = 0
         self.builds = 0
@@ -109,37 +117,75 @@ class FockServer:
                         device=self.device, precision=self.precision)
 
     def _evict_for(self, need):
-        """Evict idle engines (LRU first) until `need` bytes fit; caller holds _cv."""
-        for key in list(self._resident.keys()):
-            if self._used + need <= self.budget:
-                break
-            r = self._resident[key]
-            if r.busy:
-                continue
-            del self._resident[key]
-            self._used -= r.nbytes
-            r.engine.close()
-            self.log.append(("evict", key))
+        """Evict idle engines until `need` bytes fit; caller holds _cv.  First
+        pass: molecules with no waiting request (LRU first); second pass: any
+        idle molecule (LRU first)."""
+        for any_idle in (False, True):
+            for key in list(self._resident.keys()):
+                if self._used + need <= self.budget:
+                    return True
+                r = self._resident[key]
+                if r.busy or (not any_idle and self._waiting.get(key, 0) > 0):
+                    continue
+                del self._resident[key]
+                self._used -= r.nbytes
+                r.engine.close()
+                self.log.append(("evict", key))
         return self._used + need <= self.budget
 
+    def _take(self):
+        """Next request for a free slot (caller holds _cv): (request, resident
+        engine reserved for it, or None when the slot must admit it)."""
+        for i, (_, _, q) in enumerate(self._ready):
+            r = self._resident.get(q.key)
+            if r is not None and r.busy == 0:
+                del self._ready[i]
+                r.busy += 1
+                self._resident.move_to_end(q.key)
+                self._waiting[q.key] -= 1
+                self._taken += 1
+                return q, r
+        for i, (_, _, q) in enumerate(self._ready):
+            if q.key not in self._resident and q.key not in self._admitting:
+                del self._ready[i]
+                self._admitting.add(q.key)
+                self._waiting[q.key] -= 1
+                self._taken += 1
+                return q, None
+        return None, None
+
     def _acquire(self, req):
-        """Block until the request's engine is resident and reserved for it."""
+        """Admit the request's molecule (its key is in _admitting): block until
+        its footprint fits, then create the engine, reserved for the request."""
+        try:
+            return self._admit(req)
+        finally:
+            with self._cv:
+                self._admitting.discard(req.key)
+                self._cv.notify_all()
+
+    def _admit(self, req):
         ds, _, _ = self._systems[req.key]
         need = footprint_bytes(ds.layout, ds.nocc, self.precision)
         if need > self.budget:
             raise RuntimeError(f"molecule {req.key} needs {need / 1e9:.1f} GB > budget")
         with self._cv:
             while True:
-                r = self._resident.get(req.key)
-                if r is not None:
-                    self._resident.move_to_end(req.key)
-                    r.busy += 1
-                    return r
                 if self._evict_for(need):
                     self._used += need
                     self.max_used = max(self.max_used, self._used)
                     break
                 self._cv.wait()
+        try:
+            return self._create(req, need)
+        except BaseException:
+            with self._cv:
+                self._used -= need
+                self._cv.notify_all()
+            raise
+
+    def _create(self, req, need):
+        ds = self._systems[req.key][0]
         if getattr(ds, "B", 1) is None:
             # the host copy was dropped when an earlier engine took it: set
             # the molecule up again (only after an eviction)
@@ -199,21 +245,22 @@ class FockServer:
     def _on_setup(self, req, t0):
         req.t_setup_done = self.clock() - t0
         with self._cv:
-            heapq.heappush(self._ready, (req.arrival, req.rid, req))
+            bisect.insort(self._ready, (req.arrival, req.rid, req), key=lambda e: (e[0], e[1]))
             self._cv.notify_all()
 
     def _worker(self, t0, total):
         while True:
             with self._cv:
-                while not self._ready and self._done < total:
+                while True:
+                    req, r = self._take()
+                    if req is not None or self._taken >= total:
+                        break
                     self._cv.wait(0.05)
-                if self._done >= total and not self._ready:
-                    return
-                if not self._ready:
-                    continue
-                _, _, req = heapq.heappop(self._ready)
+            if req is None:
+                return
             try:
-                r = self._acquire(req)
+                if r is None:
+                    r = self._acquire(req)
                 try:
                     req.t_admitted = self.clock() - t0
                     ds, P, C = self._systems[req.key]
@@ -229,12 +276,18 @@ class FockServer:
             with self._cv:
                 self._done += 1
                 self.builds += req.error is None
+                done = self._done
                 self._cv.notify_all()
+            if self.progress:
+                self.progress(done, total)
 
     def run(self, requests, realtime=True):
         """Serve `requests` (arrival times relative to now); returns them."""
         reqs = sorted(requests, key=lambda q: q.arrival)
         self._done = 0
+        self._taken = 0
+        for q in reqs:
+            self._waiting[q.key] = self._waiting.get(q.key, 0) + 1
         t0 = self.clock()
         workers = [threading.Thread(target=self._worker, args=(t0, len(reqs)), daemon=True)
                    for _ in range(self.slots)]

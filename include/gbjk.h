@@ -142,6 +142,41 @@ void* gbjk_stream(gbjk_ctx* ctx);
  * No counterpart in the reference (DBCSR does not specify its order). */
 gbjk_status gbjk_k_split_plan(int nbf, int naux, int nocc, int* ksplit, long long* kchunk);
 
+/* ---- SOS-AO-MP2 Laplace batch ------------------------------------------
+ * Replaces the Z builder of megalochem's Laplace loop: mp::LL_FULL_Z
+ * (src/mp/z_full.cpp:427-620, "mi, Xmn -> Xin", "Na, XiN -> Xia", then
+ * "Xia, Yia -> XY"), driven by mpmod::compute (src/mp/mp_compute.cpp:232-382)
+ * through zbuilder->set_occ_coeff / set_vir_coeff / compute / zmat
+ * (src/mp/z_builder.hpp).  All quadrature points go in one call.
+ *
+ * Point t takes the occupied and virtual Cholesky factors of its
+ * pseudo-densities, Lo[t] (nbf x rank_o[t]) and Lv[t] (nbf x rank_v[t]),
+ * row-major host arrays (the reference's L_bu and L_br).  On the context's
+ * resident tensor, fitted with the metric's Cholesky factor
+ * ((X|mn)~ = L^-1 (X|mn), L L^T = V), it computes
+ *   Z~_t(X,Y) = sum_{i,a} W_t(X,i,a) W_t(Y,i,a),
+ *   W_t(X,i,a) = sum_{m,n} Lo_t(m,i) (X|mn)~ Lv_t(n,a),
+ * i.e. Z~_t = L^-1 Z_t L^-T of the reference's Z_t, and the Laplace term
+ *   e_t = sum_{X,Y} Z~_t(X,Y)^2 = tr(Z_t V^-1 Z_t V^-1)
+ * which the reference forms as Ztilde = Z V^-1, e_t = Ztilde . Ztilde^T
+ * (mp_compute.cpp:361-381).  The precision set by gbjk_set_precision
+ * selects the FP64 grouped GEMMs or the split-precision tensor-core path.
+ * The tensor must cover all auxiliary functions (no gbjk_set_aux_batch). */
+gbjk_status gbjk_mp2_set_factors(gbjk_ctx* ctx, int npts, const int* rank_o,
+                                 const double* const* Lo, const int* rank_v,
+                                 const double* const* Lv);
+/* Evaluate every point on the context's stream; results stay on the device. */
+gbjk_status gbjk_mp2_compute_dev(gbjk_ctx* ctx);
+/* Wait for the stream, then copy e_t (npts doubles) and, when Z is not NULL,
+ * every Z~_t (npts x naux x naux, row-major) to host memory. */
+gbjk_status gbjk_mp2_read(gbjk_ctx* ctx, double* energies, double* Z);
+/* gbjk_mp2_set_factors + gbjk_mp2_compute_dev + gbjk_mp2_read. */
+gbjk_status gbjk_mp2_laplace(gbjk_ctx* ctx, int npts, const int* rank_o, const double* const* Lo,
+                             const int* rank_v, const double* const* Lv, double* energies,
+                             double* Z);
+/* Free the batch's device buffers (the engine's tensor stays resident). */
+gbjk_status gbjk_mp2_release(gbjk_ctx* ctx);
+
 /* DF-J for callers that cannot allocate device memory — for example code
  * embedded in a host framework that owns all GPU memory through its own
  * pool, or code that must not allocate while a CUDA graph is captured.

@@ -326,3 +326,117 @@ int oracle_dfao_k(const oracle_layout* L, const double* B, const double* Vinv, c
   free(Bd);
   return 0;
 }
+
+/* ------------------------------------------------------------------------
+ * SOS-AO-MP2 Laplace term, ll_full Z builder (src/mp/z_full.cpp:427-620 and
+ * the Laplace loop src/mp/mp_compute.cpp:232-382).
+ *
+ * Per Laplace point t, with the occupied / virtual Cholesky factors Lo
+ * (nbf x r) and Lv (nbf x rv) of the pseudo-densities:
+ *   B_xov(X,i,a) = sum_{m,n} Lo(m,i) (X|mn) Lv(n,a)   ("mi, Xmn -> Xin",
+ *                                                      "Na, XiN -> Xia")
+ *   Z(X,Y)      = sum_{i,a} B_xov(X,i,a) B_xov(Y,i,a)
+ *   e_t         = tr(Z V^-1 Z V^-1)                    (mp_compute.cpp:361-381)
+ * On the prefitted tensor (X|mn)~ = L^-1 (X|mn) the same Z~ = L^-1 Z L^-T and
+ * e_t = sum_{XY} Z~(X,Y)^2 (the Cholesky route of the metric).
+ *
+ * Layouts and order follow the device path: Lo and Lv arrive zero-padded to
+ * hld and vld columns; H[n][X][i] and W[X][i][a] use those strides; every
+ * sum is an in-order fma chain; Z sums over t = i*vld + a in chunks of
+ * kchunk added in order; e = sum_X warp_dot(Z[X], Z[X]) in X order.  Only
+ * the first nx auxiliary functions are used (nx = naux: all), which bounds
+ * a timed CPU sample.
+ * ---------------------------------------------------------------------- */
+
+/* Bfit_I[m][Y][c] = sum_X Linv[Y][X] B_I[m][X][c] over X < min(naux,
+ * 64*(Y/64+1)) (entries above the diagonal are zero), in-order fma: the
+ * order of the device's lower-triangular grouped GEMM (64-row tiles). */
+void oracle_prefit(const oracle_layout* L, const double* B, const double* Linv, int nx,
+                   double* Bfit) {
+  const int naux = L->naux;
+  if (nx <= 0 || nx > naux) nx = naux;
+  for (int I = 0; I < L->nblk; ++I) {
+    const int KI = L->panel_K[I];
+    const int bI = L->blk_off[I + 1] - L->blk_off[I];
+    const double* P = B + L->panel_off[I];
+    double* Q = Bfit + L->panel_off[I];
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < (long)bI * nx; ++r) {
+      const int m = (int)(r / nx), Y = (int)(r % nx);
+      int xend = 64 * (Y / 64 + 1);
+      if (xend > naux) xend = naux;
+      const double* lrow = Linv + (size_t)Y * naux;
+      double* q = Q + ((size_t)m * naux + Y) * KI;
+      for (int c = 0; c < KI; ++c) {
+        double s = 0.0;
+        for (int X = 0; X < xend; ++X) s = fma(lrow[X], P[((size_t)m * naux + X) * KI + c], s);
+        q[c] = s;
+      }
+    }
+  }
+}
+
+int oracle_mp2_ll_point(const oracle_layout* L, const double* Bfit, const double* Lo, int hld,
+                        const double* Lv, int vld, long long kchunk, int nx, double* Z,
+                        double* e) {
+  const int n = L->nbf, naux = L->naux;
+  if (nx <= 0 || nx > naux) nx = naux;
+  const long long klen = (long long)hld * vld;
+  if (kchunk <= 0) kchunk = klen;
+  double* H = (double*)malloc(sizeof(double) * (size_t)n * nx * hld);
+  double* W = (double*)malloc(sizeof(double) * (size_t)nx * klen);
+  if (!H || !W) { free(H); free(W); return 2; }
+  /* H[mu][X][i] = sum_c Bfit_I[mu][X][c] Lo[col(c)][i] */
+  for (int I = 0; I < L->nblk; ++I) {
+    const int KI = L->panel_K[I];
+    const int bI = L->blk_off[I + 1] - L->blk_off[I];
+    const int* cm = L->colmap + L->colmap_off[I];
+    const double* P = Bfit + L->panel_off[I];
+#pragma omp parallel for schedule(static)
+    for (long r = 0; r < (long)bI * nx; ++r) {
+      const int m = (int)(r / nx), X = (int)(r % nx);
+      double* hr = H + ((size_t)(L->blk_off[I] + m) * nx + X) * hld;
+      for (int i = 0; i < hld; ++i) hr[i] = 0.0;
+      const double* br = P + ((size_t)m * naux + X) * KI;
+      for (int k = 0; k < KI; ++k) {
+        const double b = br[k];
+        const double* c = Lo + (size_t)cm[k] * hld;
+        for (int i = 0; i < hld; ++i) hr[i] = fma(b, c[i], hr[i]);
+      }
+    }
+  }
+  /* W[X][i][a] = sum_n H[n][X][i] Lv[n][a] */
+#pragma omp parallel for schedule(static)
+  for (long r = 0; r < (long)nx * hld; ++r) {
+    const int X = (int)(r / hld), i = (int)(r % hld);
+    double* w = W + (size_t)r * vld;
+    for (int a = 0; a < vld; ++a) w[a] = 0.0;
+    for (int mu = 0; mu < n; ++mu) {
+      const double h = H[((size_t)mu * nx + X) * hld + i];
+      const double* lv = Lv + (size_t)mu * vld;
+      for (int a = 0; a < vld; ++a) w[a] = fma(h, lv[a], w[a]);
+    }
+  }
+  /* Z[X][Y] (X <= Y, mirrored) */
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int X = 0; X < nx; ++X)
+    for (int Y = X; Y < nx; ++Y) {
+      const double* a = W + (size_t)X * klen;
+      const double* b = W + (size_t)Y * klen;
+      double s = 0.0;
+      for (long long t0 = 0; t0 < klen; t0 += kchunk) {
+        const long long t1 = t0 + kchunk < klen ? t0 + kchunk : klen;
+        double p = 0.0;
+        for (long long t = t0; t < t1; ++t) p = fma(a[t], b[t], p);
+        s += p;
+      }
+      Z[(size_t)X * nx + Y] = s;
+      Z[(size_t)Y * nx + X] = s;
+    }
+  double acc = 0.0;
+  for (int X = 0; X < nx; ++X) acc += warp_dot(Z + (size_t)X * nx, Z + (size_t)X * nx, nx, 1);
+  *e = acc;
+  free(H);
+  free(W);
+  return 0;
+}

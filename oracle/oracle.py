@@ -56,6 +56,9 @@ def lib():
         L.oracle_dfao_k.argtypes = [lp, dp, dp, dp, dp, C.c_double]
         L.oracle_half_transform.argtypes = [lp, dp, dp, C.c_int, dp]
         L.oracle_filter.argtypes = [lp, dp, C.c_double]
+        L.oracle_prefit.argtypes = [lp, dp, dp, C.c_int, dp]
+        L.oracle_mp2_ll_point.argtypes = [lp, dp, dp, C.c_int, dp, C.c_int, C.c_longlong,
+                                          C.c_int, dp, dp]
         _lib = L
     return _lib
 
@@ -138,6 +141,33 @@ class Oracle:
         lib().oracle_half_transform(C.byref(self.L), _dp(self.B), _dp(Cocc), Cocc.shape[1], _dp(H))
         return H
 
+    def prefit(self, Linv, nx=0):
+        """L^-1 B per panel in the device's lower-triangular GEMM order; only
+        the first nx auxiliary rows when nx > 0 (the rest stay zero)."""
+        Bf = np.zeros_like(self.B)
+        lib().oracle_prefit(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Linv)),
+                            int(nx), _dp(Bf))
+        return Bf
+
+    def mp2_ll_point(self, Bfit, Lo, Lv, kchunk=0, nx=0):
+        """(Z~, e) of one Laplace point (ll_full builder) on the prefitted
+        tensor, in the device path's padded layouts and summation order.
+        nx > 0 restricts to the first nx auxiliary functions."""
+        n = self.layout.nbf
+        ro, rv = Lo.shape[1], Lv.shape[1]
+        hld, vld = ro + (ro & 1), rv + (rv & 1)
+        lo = np.zeros((n, hld)); lo[:, :ro] = Lo
+        lv = np.zeros((n, vld)); lv[:, :rv] = Lv
+        m = nx if 0 < nx < self.layout.naux else self.layout.naux
+        Z = np.zeros((m, m))
+        e = C.c_double()
+        rc = lib().oracle_mp2_ll_point(C.byref(self.L), _dp(np.ascontiguousarray(Bfit)), _dp(lo),
+                                       hld, _dp(lv), vld, int(kchunk), int(nx), _dp(Z),
+                                       C.byref(e))
+        if rc:
+            raise MemoryError("oracle_mp2_ll_point")
+        return Z, e.value
+
     def filter(self, M, eps):
         M = np.ascontiguousarray(M, float).copy()
         lib().oracle_filter(C.byref(self.L), _dp(M), eps)
@@ -167,3 +197,38 @@ def dense_dfao_k(T, Vinv, P):
     cbar = np.einsum("xmn,nl->xml", T, P)
     c = np.einsum("xy,yns->xns", Vinv, T)
     return -np.einsum("xns,xms->mn", c, cbar)
+
+
+# --- SOS-AO-MP2 Laplace term (dense numpy restatements) -------------------
+
+def dense_mp2_ll(T, Vinv, Lo, Lv):
+    """ll_full route (src/mp/z_full.cpp:427-620): B_xov = Lo^T (X|mn) Lv,
+    Z = B_xov B_xov^T, e = tr(Z V^-1 Z V^-1) (mp_compute.cpp:361-381)."""
+    W = np.einsum("mi,xmn,na->xia", Lo, T, Lv, optimize=True)
+    Z = np.einsum("xia,yia->xy", W, W, optimize=True)
+    Zt = Z @ Vinv
+    return Z, float(np.sum(Zt * Zt.T))
+
+
+def dense_mp2_llmp(T, Vinv, Lo, Pv, pair_mask):
+    """llmp_full route, megalochem's default Z builder (z_full.cpp:69-397):
+    B = Lo^T (X|mn), B2 = B Pv, B3 = Lo B2 kept on the screened shell-pair
+    pattern, Z(X,Y) = sum_mn B3(X,m,n) (Y|mn)."""
+    B1 = np.einsum("mi,xmn->xin", Lo, T, optimize=True)
+    B2 = np.einsum("Nn,xin->xiN", Pv, B1, optimize=True)
+    B3 = np.einsum("Mi,xiN->xMN", Lo, B2, optimize=True) * pair_mask[None]
+    Z = np.einsum("xmn,ymn->xy", B3, T, optimize=True)
+    Zt = Z @ Vinv
+    return Z, float(np.sum(Zt * Zt.T))
+
+
+def dense_sos_mp2(T, Vinv, C_occ, C_vir, e_occ, e_vir):
+    """sum_{ijab} (ia|jb)^2 / (e_a + e_b - e_i - e_j) with DF integrals: the
+    quantity the Laplace sum of e_t approximates."""
+    Bia = np.einsum("xmn,mi,na->xia", T, C_occ, C_vir, optimize=True)
+    Lc = np.linalg.cholesky(Vinv)
+    Q = np.einsum("xy,xia->yia", Lc, Bia, optimize=True)
+    iajb = np.einsum("yia,yjb->iajb", Q, Q, optimize=True)
+    den = (e_vir[None, :, None, None] + e_vir[None, None, None, :]
+           - e_occ[:, None, None, None] - e_occ[None, None, :, None])
+    return float(np.sum(iajb ** 2 / den))

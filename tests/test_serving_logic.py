@@ -64,3 +64,41 @@ def test_oversized_request_is_an_error_not_a_hang():
     done = srv.run([Request(0, "x", 0.0, lambda: (ds, np.eye(40), np.ones((40, 5))))])
     srv.close()
     assert done[0].error and "budget" in done[0].error
+
+
+def test_requests_of_a_resident_molecule_are_served_together():
+    # budget for one molecule at a time; requests alternate a, b, a, b, ...
+    # and all arrive before any set-up ends: each molecule is admitted once
+    sizes = {"a": (40, 200, 5), "b": (44, 220, 5)}
+    systems = {k: (_DS(*v), np.eye(v[0]), np.ones((v[0], v[2]))) for k, v in sizes.items()}
+    need = max(footprint_bytes(s[0].layout, s[0].nocc) for s in systems.values())
+
+    def slow(k):
+        time.sleep(0.05)
+        return systems[k]
+
+    srv = FockServer(budget_bytes=need, slots=2, engine_factory=_FakeEngine)
+    reqs = [Request(i, "ab"[i % 2], 0.0, lambda k="ab"[i % 2]: slow(k)) for i in range(12)]
+    done = srv.run(reqs, realtime=False)
+    srv.close()
+    assert all(q.error is None for q in done)
+    admits = [e for e in srv.log if e[0] == "admit"]
+    assert len(admits) == 2, srv.log
+    assert srv.max_used <= need
+
+
+def test_no_double_admission_with_many_slots():
+    ds = _DS(40, 200, 5)
+    created = []
+
+    def factory(d):
+        created.append(1)
+        return _FakeEngine(d)
+
+    srv = FockServer(budget_bytes=10 * footprint_bytes(ds.layout, ds.nocc), slots=4,
+                     engine_factory=factory)
+    reqs = [Request(i, "x", 0.0, lambda: (ds, np.eye(40), np.ones((40, 5)))) for i in range(16)]
+    done = srv.run(reqs, realtime=False)
+    srv.close()
+    assert all(q.error is None for q in done)
+    assert len(created) == 1
