@@ -75,7 +75,7 @@ struct gbjk_ctx {
   double *d_Linv = nullptr, *d_Vinv = nullptr;
   bool have_B = false, have_metric = false;
   bool fitted = false;  // the uploaded tensor already is L^-1 B (no metric)
-  bool colsum_smem_set = false;
+  bool colsum_smem_set = false, colsum2_smem_set = false;
   // J workspace
   double *d_P = nullptr, *d_Pg = nullptr, *d_part = nullptr, *d_g = nullptr, *d_h = nullptr,
          *d_y = nullptr, *d_J = nullptr;
@@ -756,13 +756,13 @@ static gbjk_status run_jk_split(gbjk_ctx* ctx, const double* dP, const double* d
   }
   {
     PhaseScope ps(ctx, PH_J_COLSUM);
-    const size_t hbytes = (size_t)naux * sizeof(double);
-    if (hbytes > 48 * 1024 && !ctx->colsum_smem_set) {
-      CK(cudaFuncSetAttribute(k_j_colsum, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const size_t hbytes = (size_t)naux * sizeof(float2);
+    if (hbytes > 48 * 1024 && !ctx->colsum2_smem_set) {
+      CK(cudaFuncSetAttribute(k_j_colsum_f32x2, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)hbytes));
-      ctx->colsum_smem_set = true;
+      ctx->colsum2_smem_set = true;
     }
-    k_j_colsum<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, hbytes, ctx->stream>>>(
+    k_j_colsum_f32x2<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, hbytes, ctx->stream>>>(
         ctx->split.Bfit, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK,
         ctx->d_cmoff, ctx->d_colmap, ctx->split.d_dt, nbf, naux, dJ);
     CKL(PH_J_COLSUM);

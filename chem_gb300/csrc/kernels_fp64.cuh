@@ -112,6 +112,20 @@ __global__ void k_j_colsum(const double* __restrict__ B, const long long* __rest
   const double* b = B + panel_off[I] + (long long)m * naux * KI + k;
   double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
   int X = 0;
+  // eight loads in flight per thread; accumulator X % 4, in X order
+  for (; X + 7 < naux; X += 8) {
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __ldg(b + (long long)(X + j) * KI);
+    s0 = fma(v[0], hs[X], s0);
+    s1 = fma(v[1], hs[X + 1], s1);
+    s2 = fma(v[2], hs[X + 2], s2);
+    s3 = fma(v[3], hs[X + 3], s3);
+    s0 = fma(v[4], hs[X + 4], s0);
+    s1 = fma(v[5], hs[X + 5], s1);
+    s2 = fma(v[6], hs[X + 6], s2);
+    s3 = fma(v[7], hs[X + 7], s3);
+  }
   for (; X + 3 < naux; X += 4) {
     s0 = fma(b[(long long)X * KI], hs[X], s0);
     s1 = fma(b[(long long)(X + 1) * KI], hs[X + 1], s1);
@@ -120,6 +134,103 @@ __global__ void k_j_colsum(const double* __restrict__ B, const long long* __rest
   }
   for (; X < naux; ++X) s0 = fma(b[(long long)X * KI], hs[X], s0);
   J[(long long)mu * nbf + colmap[cmoff[I] + k]] = (s0 + s1) + (s2 + s3);
+}
+
+// x as hi + lo, two FP32 values built from the FP64 bit pattern with
+// integer operations (no FP64 instruction): hi = the top 24 significand bits
+// (truncated), lo = the remaining 29 bits rounded to FP32.  |x| < 2^-126
+// gives (0, 0) and a lo below FP32's normal range gives lo = 0; both are
+// below 2^-100 relative to the O(1) sums they enter.
+__device__ __forceinline__ void f64_split_f32(double x, float& hi, float& lo) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const int E = (int)((u >> 52) & 0x7FF);
+  const unsigned int sgn = (unsigned int)(u >> 32) & 0x80000000u;
+  const int ef = E - 896;  // FP32 biased exponent of hi (E - 1023 + 127)
+  if (ef < 1 || ef > 254) {
+    hi = 0.f;
+    lo = 0.f;
+    return;
+  }
+  hi = __uint_as_float(sgn | ((unsigned int)ef << 23) | (unsigned int)((u >> 29) & 0x7FFFFF));
+  // lo = m29 * 2^(E - 1075): the scale 2^(E-1075) as an FP32 bit pattern
+  const int es = E - 1075 + 127;
+  if (es < 1) {
+    lo = 0.f;
+    return;
+  }
+  const float m29 = (float)(unsigned int)(u & 0x1FFFFFFFu);
+  lo = __uint_as_float(sgn | ((unsigned int)es << 23)) * m29;
+}
+
+// Mixed-path J columns: J[mu][colmap[k]] = sum_X B_I[m][X][k] h[X] with the
+// products and the sum in FP32 pairs (hi/lo operands, exact product error
+// by fma, TwoSum accumulation): about 46 significant bits, no FP64
+// arithmetic in the loop, so the pass runs at HBM speed rather than at
+// GB300's FP64 rate.  grid (ceil(maxK/128), nbf), dynamic smem naux float2.
+__global__ void k_j_colsum_f32x2(const double* __restrict__ B,
+                                 const long long* __restrict__ panel_off,
+                                 const int* __restrict__ blk_of, const int* __restrict__ boff,
+                                 const int* __restrict__ panel_K, const int* __restrict__ cmoff,
+                                 const int* __restrict__ colmap, const double* __restrict__ h,
+                                 int nbf, int naux, double* __restrict__ J) {
+  extern __shared__ float2 h2[];
+  for (int x = threadIdx.x; x < naux; x += blockDim.x) {
+    float a, b;
+    f64_split_f32(h[x], a, b);
+    h2[x] = make_float2(a, b);
+  }
+  __syncthreads();
+  const int mu = blockIdx.y;
+  const int I = blk_of[mu];
+  const int m = mu - boff[I];
+  const int KI = panel_K[I];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= KI) return;
+  const double* bp = B + panel_off[I] + (long long)m * naux * KI + k;
+  float sh0 = 0.f, sl0 = 0.f, se0 = 0.f, sh1 = 0.f, sl1 = 0.f, se1 = 0.f;
+  // explicit round-to-nearest intrinsics: no multiply-add contraction may
+  // merge the product into the TwoSum
+  auto acc = [](float bh, float bl, float2 hh, float& sh, float& sl, float& se) {
+    const float p = __fmul_rn(bh, hh.x);
+    float e = fmaf(bh, hh.x, -p);
+    e = fmaf(bh, hh.y, e);
+    e = fmaf(bl, hh.x, e);
+    const float t = __fadd_rn(sh, p);
+    const float z = __fsub_rn(t, sh);
+    sl = __fadd_rn(sl, __fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(p, z)));
+    sh = t;
+    se = __fadd_rn(se, e);
+  };
+  int X = 0;
+  // eight loads in flight per thread
+  for (; X + 7 < naux; X += 8) {
+    double v[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) v[j] = __ldg(bp + (long long)(X + j) * KI);
+#pragma unroll
+    for (int j = 0; j < 8; j += 2) {
+      float b0h, b0l, b1h, b1l;
+      f64_split_f32(v[j], b0h, b0l);
+      f64_split_f32(v[j + 1], b1h, b1l);
+      acc(b0h, b0l, h2[X + j], sh0, sl0, se0);
+      acc(b1h, b1l, h2[X + j + 1], sh1, sl1, se1);
+    }
+  }
+  for (; X + 1 < naux; X += 2) {
+    float b0h, b0l, b1h, b1l;
+    f64_split_f32(bp[(long long)X * KI], b0h, b0l);
+    f64_split_f32(bp[(long long)(X + 1) * KI], b1h, b1l);
+    acc(b0h, b0l, h2[X], sh0, sl0, se0);
+    acc(b1h, b1l, h2[X + 1], sh1, sl1, se1);
+  }
+  if (X < naux) {
+    float bh, bl;
+    f64_split_f32(bp[(long long)X * KI], bh, bl);
+    acc(bh, bl, h2[X], sh0, sl0, se0);
+  }
+  const double s = ((double)sh0 + (double)sh1) + (((double)sl0 + (double)sl1) +
+                                                   ((double)se0 + (double)se1));
+  J[(long long)mu * nbf + colmap[cmoff[I] + k]] = s;
 }
 
 // Grouped FP64 GEMM over a tile list; 64x64 tiles, 256 threads, 4x4 per thread.
