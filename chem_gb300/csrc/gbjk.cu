@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "gbjk.h"
+#include "aok_host.cuh"
 #include "kernels_fp64.cuh"
 #include "mp2_host.cuh"
 #include "split_host.cuh"
@@ -98,6 +99,8 @@ struct gbjk_ctx {
   SplitState split;
   // SOS-AO-MP2 Laplace batch (ll_full Z builder) on the prefitted tensor
   Mp2State mp2;
+  // DF-AO exchange (fitted coefficients, dense intermediates)
+  AoKState aok;
   // profiling
   bool profile = false;
   cudaEvent_t ev[PH_COUNT][2] = {};
@@ -591,6 +594,7 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->mp2.release();
+  ctx->aok.release();
   ctx->split.release();
   void* ptrs[] = {ctx->d_blk_of, ctx->d_boff,  ctx->d_panelK, ctx->d_cmoff, ctx->d_colmap,
                   ctx->d_panel_off, ctx->d_pg_off, ctx->d_B, ctx->d_Linv, ctx->d_Vinv,
@@ -621,6 +625,7 @@ gbjk_status gbjk_upload_b(gbjk_ctx* ctx, const double* B) {
   ctx->have_B = true;
   ctx->ws_nocc = -1;  // plans hold d_B
   ctx->mp2.release();
+  ctx->aok.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -636,6 +641,7 @@ gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* 
   ctx->have_metric = true;
   ctx->ws_nocc = -1;
   ctx->mp2.release();
+  ctx->aok.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -656,6 +662,7 @@ gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
   ctx->fitted = fitted != 0;
   ctx->split.fitted = ctx->fitted;
   ctx->mp2.release();
+  ctx->aok.release();
   ctx->split.invalidate_b();
   ctx->ws_nocc = -1;  // exchange plan reads H or the fitted H
   return GBJK_OK;
@@ -665,6 +672,7 @@ gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows) {
   if (!ctx || rows < 0) return GBJK_INVALID_ARG;
   ctx->split.xb_req = rows;
   ctx->mp2.release();
+  ctx->aok.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -685,6 +693,7 @@ gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, doub
   ctx->have_B = true;
   ctx->ws_nocc = -1;
   ctx->mp2.release();
+  ctx->aok.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -888,7 +897,7 @@ gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int n
 }
 
 size_t gbjk_device_bytes(const gbjk_ctx* ctx) {
-  return ctx ? ctx->dev_bytes + ctx->split.bytes + ctx->mp2.bytes : 0;
+  return ctx ? ctx->dev_bytes + ctx->split.bytes + ctx->mp2.bytes + ctx->aok.bytes : 0;
 }
 int64_t gbjk_kernel_launches(const gbjk_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
@@ -920,6 +929,61 @@ int gbjk_profile_read(const gbjk_ctx* ctx, int idx, const char** name, double* m
   gbjk_ctx* c = const_cast<gbjk_ctx*>(ctx);
   if (c->split.profile_read(idx - PH_COUNT, name, ms, launches)) return 1;
   return c->mp2.profile_read(idx - PH_COUNT - 4, name, ms, launches);
+}
+
+// --- DF-AO exchange -------------------------------------------------------------
+
+static AoKState::Layout aok_layout(gbjk_ctx* ctx) {
+  AoKState::Layout L;
+  L.nbf = ctx->nbf;
+  L.naux = ctx->naux;
+  L.nblk = ctx->nblk;
+  L.ncols_total = ctx->ncols_total;
+  L.maxK = ctx->maxK;
+  L.bsize = &ctx->bsize;
+  L.boff = &ctx->boff;
+  L.panelK = &ctx->panelK;
+  L.cmoff = &ctx->cmoff;
+  L.panel_off = &ctx->panel_off;
+  L.d_blk_of = ctx->d_blk_of;
+  L.d_boff = ctx->d_boff;
+  L.d_panelK = ctx->d_panelK;
+  L.d_cmoff = ctx->d_cmoff;
+  L.d_colmap = ctx->d_colmap;
+  L.d_panel_off = ctx->d_panel_off;
+  return L;
+}
+
+gbjk_status gbjk_compute_k_ao_dev(gbjk_ctx* ctx, const double* dP, double* dK) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (!dP || !dK) return fail(ctx, GBJK_INVALID_ARG, "gbjk_compute_k_ao_dev: null argument");
+  const AoKState::Layout L = aok_layout(ctx);
+  if (ctx->precision == GBJK_SPLIT_BF16 && !ctx->split.b_ready &&
+      (s = ctx->split.prepare_b(ctx->stream, ctx->d_B, ctx->d_Linv, &ctx->launches, &ctx->err)))
+    return s;
+  if ((s = ctx->aok.prepare(ctx->stream, ctx->precision, L, ctx->d_B,
+                            ctx->fitted ? nullptr : ctx->d_Vinv, ctx->split, &ctx->launches,
+                            &ctx->err)))
+    return s;
+  {
+    PhaseScope ps(ctx, PH_KGEMM);
+    if ((s = ctx->aok.run(ctx->stream, L, dP, dK, ctx->split, &ctx->launches, &ctx->err)))
+      return s;
+  }
+  return filter(ctx, dK);
+}
+
+gbjk_status gbjk_compute_k_ao(gbjk_ctx* ctx, const double* P, double* K) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (!P || !K) return fail(ctx, GBJK_INVALID_ARG, "gbjk_compute_k_ao: null argument");
+  if ((s = ensure_j_workspace(ctx))) return s;
+  const size_t n2 = (size_t)ctx->nbf * ctx->nbf;
+  CK(cudaMemcpyAsync(ctx->d_P, P, n2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  if ((s = gbjk_compute_k_ao_dev(ctx, ctx->d_P, ctx->d_K))) return s;
+  CK(cudaMemcpyAsync(K, ctx->d_K, n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  return gbjk_synchronize(ctx);
 }
 
 // --- SOS-AO-MP2 Laplace batch -----------------------------------------------

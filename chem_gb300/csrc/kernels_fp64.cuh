@@ -233,6 +233,24 @@ __global__ void k_j_colsum_f32x2(const double* __restrict__ B,
   J[(long long)mu * nbf + colmap[cmoff[I] + k]] = s;
 }
 
+// Dense expansion of the panel array: D[mu][X][colmap(k)] = P_I[m][X][k]
+// (mu = boff[I] + m); entries outside the kept pattern are not written.
+// grid (ceil(maxK/128), naux, nbf).
+__global__ void k_expand_panels(const double* __restrict__ P, const long long* __restrict__ panel_off,
+                                const int* __restrict__ blk_of, const int* __restrict__ boff,
+                                const int* __restrict__ panel_K, const int* __restrict__ cmoff,
+                                const int* __restrict__ colmap, int nbf, int naux,
+                                double* __restrict__ D) {
+  const int mu = blockIdx.z, X = blockIdx.y;
+  const int I = blk_of[mu];
+  const int KI = panel_K[I];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= KI) return;
+  const int m = mu - boff[I];
+  D[((long long)mu * naux + X) * nbf + colmap[cmoff[I] + k]] =
+      P[panel_off[I] + ((long long)m * naux + X) * KI + k];
+}
+
 // Grouped FP64 GEMM over a tile list; 64x64 tiles, 256 threads, 4x4 per thread.
 // TRANSA: A is stored K x M row-major, op(A)(m, k) = A[k * lda + m].
 template <bool TRANSB, bool TRANSA = false>

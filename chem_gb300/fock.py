@@ -23,7 +23,7 @@ _lib = None
 
 GBJK_FP64 = 0
 GBJK_SPLIT_BF16 = 1
-KMETHODS = {"dfmo": 0, "dflmo": 1}
+KMETHODS = {"dfmo": 0, "dflmo": 1}  # coefficient-based; "dfao" takes the density
 JMETHODS = ("dfao",)
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT",
           5: "NOT_CONVERGED", 6: "NOT_READY"}
@@ -64,6 +64,8 @@ def lib():
         L.gbjk_compute_j.argtypes = [vp, dp, dp]
         L.gbjk_compute_k.argtypes = [vp, C.c_int, dp, C.c_int, dp]
         L.gbjk_compute_jk.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, dp]
+        L.gbjk_compute_k_ao.argtypes = [vp, dp, dp]
+        L.gbjk_compute_k_ao_dev.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.gbjk_compute_jk_dev.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                           C.c_void_p, C.c_void_p]
         L.gbjk_synchronize.argtypes = [vp]
@@ -185,6 +187,16 @@ class JKEngine:
             _dp(J) if J is not None else None, _dp(K) if K is not None else None),
             "gbjk_compute_jk")
         return J, K
+
+    def compute_k_ao(self, P):
+        """DF-AO K (gbjk_compute_k_ao) from the alpha density P; K negated."""
+        P = np.ascontiguousarray(P, float)
+        K = np.zeros((self.nbf, self.nbf))
+        self._check(lib().gbjk_compute_k_ao(self.h, _dp(P), _dp(K)), "gbjk_compute_k_ao")
+        return K
+
+    def compute_k_ao_dev(self, dP, dK):
+        self._check(lib().gbjk_compute_k_ao_dev(self.h, dP, dK), "gbjk_compute_k_ao_dev")
 
     def compute_jk_dev(self, dP, dC, nocc, dJ, dK, kmethod="dfmo"):
         """Device pointers (ints); ordered on the engine stream, no sync."""
@@ -360,6 +372,17 @@ class DFLMO_K(_DFK):
     kmethod = "dflmo"
 
 
+class DFAO_K(K):
+    """fock::DFAO_K (src/fock/jkdf.cpp:464-648): K from the alpha (and beta)
+    density with the fitting coefficients V^-1 (X|mn)."""
+
+    def compute_K(self):
+        if self.m_p_A is None:
+            raise RuntimeError("DFAO_K: density not set")
+        self.m_K_A = self.engine.compute_k_ao(self.m_p_A)
+        self.m_K_B = None if self.m_p_B is None else self.engine.compute_k_ao(self.m_p_B)
+
+
 def create_j(engine: JKEngine, method="dfao") -> J:
     """fock::create_j (src/fock/jkbuilder.hpp:621-690)."""
     if method not in JMETHODS:
@@ -373,4 +396,6 @@ def create_k(engine: JKEngine, method="dfmo") -> K:
         return DFMO_K(engine)
     if method == "dflmo":
         return DFLMO_K(engine)
+    if method == "dfao":
+        return DFAO_K(engine)
     raise RuntimeError("Invalid kmethod")

@@ -51,7 +51,7 @@ typedef enum {
 typedef enum { GBJK_FP64 = 0, GBJK_SPLIT_BF16 = 1 } gbjk_precision;
 
 /* K builder, by the reference's kmethod strings (src/fock/jkbuilder.hpp:37-60) */
-typedef enum { GBJK_K_DFMO = 0, GBJK_K_DFLMO = 1 } gbjk_kmethod;
+typedef enum { GBJK_K_DFMO = 0, GBJK_K_DFLMO = 1, GBJK_K_DFAO = 2 } gbjk_kmethod;
 
 /* Route of the FP64 J's metric step.  GBJK_J_VINV multiplies by the
  * explicit inverse V^-1 = L^-T L^-1, as fock::DF_J does
@@ -117,6 +117,17 @@ gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode);
 gbjk_status gbjk_compute_j(gbjk_ctx* ctx, const double* Ptot, double* J);
 /* K_{mu nu} = -sum_{X,i} Bfit_{X mu i} Bfit_{X nu i}, Cocc is nbf x nocc. */
 gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int nocc, double* K);
+/* DF-AO K (fock::DFAO_K, src/fock/jkdf.cpp:464-648, with the fitting
+ * coefficients of ints::dfitting, src/ints/fitting.cpp:44-161):
+ *   K_{MN} = -sum_{X,S} c_{XNS} cbar_{XMS},  cbar = (X|MN) P_{NS},
+ *   c = V^-1 (Y|NS),
+ * from the alpha density P (nbf x nbf, the builder's set_density_alpha).
+ * The FP64 path follows that route (c fitted once per tensor, kept dense
+ * over S); the split path uses the Cholesky route,
+ *   K = -sum_{Y,S} [L^-1 B]_{YNS} [L^-1 cbar]_{YMS}.
+ * Host and device-pointer (stream-ordered) forms. */
+gbjk_status gbjk_compute_k_ao(gbjk_ctx* ctx, const double* P, double* K);
+gbjk_status gbjk_compute_k_ao_dev(gbjk_ctx* ctx, const double* dP, double* dK);
 /* One Fock build: J from Ptot and K from Cocc in one call. */
 gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* Ptot, const double* Cocc,
                             int nocc, double* J, double* K);

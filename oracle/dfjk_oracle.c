@@ -298,7 +298,7 @@ int oracle_dflmo_k(const oracle_layout* L, const double* B, const double* Vinv, 
 /* DF-AO K: cbar[X][M][L] = sum_N (X|MN) P_NL, c = V^-1 (X|..),
  * K_MN = -sum_{X,S} c[X][N][S] cbar[X][M][S]  (jkdf.cpp:549-615). */
 int oracle_dfao_k(const oracle_layout* L, const double* B, const double* Vinv, const double* P,
-                  double* K, double eps) {
+                  double* K, double eps, long long kchunk) {
   const int n = L->nbf;
   /* cbar via the half transform with C := P (n columns) */
   const size_t sz = (size_t)n * L->naux * n;
@@ -319,7 +319,7 @@ int oracle_dfao_k(const oracle_layout* L, const double* B, const double* Vinv, c
       }
   }
   apply_metric(L, Vinv, 0, Bd, n, c); /* c[N][X][S] = sum_Y Vinv[X][Y] B[N][Y][S] */
-  contract_k(L, cbar, c, n, K, 0, 0);  /* K[M][N] = -sum_{X,S} cbar[M][X][S] c[N][X][S] */
+  contract_k(L, cbar, c, n, K, 0, kchunk);  /* K[M][N] = -sum_{X,S} cbar[M][X][S] c[N][X][S] */
   oracle_filter(L, K, eps);
   free(cbar);
   free(c);

@@ -53,7 +53,7 @@ def lib():
         L.oracle_df_j_chol.argtypes = [lp, dp, dp, dp, dp, C.c_double]
         L.oracle_dfmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
         L.oracle_dflmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
-        L.oracle_dfao_k.argtypes = [lp, dp, dp, dp, dp, C.c_double]
+        L.oracle_dfao_k.argtypes = [lp, dp, dp, dp, dp, C.c_double, C.c_longlong]
         L.oracle_half_transform.argtypes = [lp, dp, dp, C.c_int, dp]
         L.oracle_filter.argtypes = [lp, dp, C.c_double]
         L.oracle_prefit.argtypes = [lp, dp, dp, C.c_int, dp]
@@ -125,11 +125,13 @@ class Oracle:
             raise MemoryError("oracle_dflmo_k")
         return K
 
-    def dfao_k(self, Vinv, P, eps=0.0):
+    def dfao_k(self, Vinv, P, eps=0.0, kchunk=0):
+        """kchunk: in-order partial sums of the exchange over t = (X, S)
+        (the device path uses chem_gb300.fock.k_split_plan(nbf, naux, nbf))."""
         n = self.layout.nbf
         K = np.zeros((n, n))
         rc = lib().oracle_dfao_k(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Vinv)),
-                                 _dp(np.ascontiguousarray(P)), _dp(K), eps)
+                                 _dp(np.ascontiguousarray(P)), _dp(K), eps, int(kchunk))
         if rc:
             raise MemoryError("oracle_dfao_k")
         return K
