@@ -41,6 +41,7 @@ def parse():
     ap.add_argument("--kmethod", default="dfmo")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scf", action="store_true")
+    ap.add_argument("--no-dfao", action="store_true")
     ap.add_argument("--workload", default="fock", choices=["fock", "serving", "synthetic", "mp2"])
     ap.add_argument("--mp2-alkane", type=int, default=40)
     ap.add_argument("--mp2-points", type=int, default=8)
@@ -627,6 +628,36 @@ def main():
                                  "of one Fock build at the bench density (E = sum P_alpha "
                                  "(H + F), F = H + J + K)"}
 
+    # DF-AO K (the reference example's K builder) at the same density: split
+    # and FP64 build times, and agreement with DF-MO K of the same density
+    dfao = None
+    if args.precision == "split" and not args.no_dfao:
+        Pa = np.ascontiguousarray(P)
+        dPa = torch.from_numpy(Pa).to(dev)
+        dKa = torch.empty((n, n), dtype=torch.float64, device=dev)
+        res = {}
+        for prec in ("split", "fp64"):
+            eng.set_precision(prec)
+            eng.compute_k_ao_dev(dPa.data_ptr(), dKa.data_ptr())  # plan, fitting, warm-up
+            eng.synchronize()
+            nst = 3 if prec == "fp64" else max(3, args.steps)
+            a0 = torch.cuda.Event(enable_timing=True)
+            a1 = torch.cuda.Event(enable_timing=True)
+            a0.record(stream)
+            for _ in range(nst):
+                eng.compute_k_ao_dev(dPa.data_ptr(), dKa.data_ptr())
+            a1.record(stream)
+            eng.synchronize()
+            res[prec] = (a0.elapsed_time(a1) / nst, dKa.cpu().numpy())
+        eng.set_precision("fp64")
+        _, Kmo64 = eng.compute_jk(None, Cocc, "dfmo")
+        eng.set_precision(args.precision)
+        dfao = {"split_ms": res["split"][0], "fp64_ms": res["fp64"][0],
+                "speedup": res["fp64"][0] / res["split"][0],
+                "max_abs_dK_split_vs_fp64_dfmo": float(np.abs(res["split"][1] - Kmo64).max()),
+                "max_abs_dK_fp64_dfao_vs_fp64_dfmo": float(np.abs(res["fp64"][1] - Kmo64).max()),
+                "dE_K_split_vs_fp64_Eh": float(np.sum(P * (res["split"][1] - res["fp64"][1])))}
+
     # full DF-HF SCF (the config's SCF comparison): FP64 on the reference
     # route, FP64 on the Cholesky route, mixed precision switching to FP64
     # (Cholesky route) once the DIIS error is below 1e-5
@@ -685,6 +716,7 @@ def main():
         "gpu_launches": int(launches),
         "roofline": roof,
         "fp64_gpu": fp64,
+        "dfao_k": dfao,
         "scf": scf,
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[1]},
         "clocks": clk.summary(),

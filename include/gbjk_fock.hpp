@@ -129,6 +129,58 @@ class DF_K : public K {
   int kmethod_;
 };
 
+// fock::DFAO_K (src/fock/jkdf.cpp:464-648): K from the density with the
+// fitting coefficients V^-1 (X|mn) (src/ints/fitting.cpp:44-161).
+class DFAO_K : public K {
+ public:
+  using K::K;
+  void init() override {
+    const size_t n2 = (size_t)eng_->nbf() * eng_->nbf();
+    m_K_A = std::make_shared<std::vector<double>>(n2);
+    if (m_p_B) m_K_B = std::make_shared<std::vector<double>>(n2);
+  }
+  void compute_K() override {
+    if (!m_p_A) throw std::runtime_error("DFAO_K: density not set");
+    eng_->check(gbjk_compute_k_ao(eng_->ctx(), m_p_A->data(), m_K_A->data()), "DFAO_K::compute_K");
+    if (m_p_B) {
+      if (!m_K_B) m_K_B = std::make_shared<std::vector<double>>(m_K_A->size());
+      eng_->check(gbjk_compute_k_ao(eng_->ctx(), m_p_B->data(), m_K_B->data()),
+                  "DFAO_K::compute_K");
+    }
+  }
+};
+
+// mp::LL_FULL_Z (src/mp/z_full.cpp:427-620) for all Laplace points at once:
+// set_occ_coeff / set_vir_coeff per point (nbf x rank, row-major), then
+// compute(); energies() holds e_t = tr(Z_t V^-1 Z_t V^-1), zmat(t) the
+// fitted Z~_t = L^-1 Z_t L^-T (naux x naux) when requested.
+class LaplaceZ {
+ public:
+  LaplaceZ(std::shared_ptr<engine> e, int npts)
+      : eng_(std::move(e)), lo_(npts), lv_(npts), ro_(npts, 0), rv_(npts, 0), e_(npts, 0.0) {}
+  void set_occ_coeff(int t, matrix L, int rank) { lo_.at(t) = std::move(L); ro_.at(t) = rank; }
+  void set_vir_coeff(int t, matrix L, int rank) { lv_.at(t) = std::move(L); rv_.at(t) = rank; }
+  void compute(std::vector<double>* zmats = nullptr) {
+    const int n = (int)lo_.size();
+    std::vector<const double*> po(n), pv(n);
+    for (int t = 0; t < n; ++t) {
+      if (!lo_[t] || !lv_[t]) throw std::runtime_error("LaplaceZ: factor not set");
+      po[t] = lo_[t]->data();
+      pv[t] = lv_[t]->data();
+    }
+    eng_->check(gbjk_mp2_laplace(eng_->ctx(), n, ro_.data(), po.data(), rv_.data(), pv.data(),
+                                 e_.data(), zmats ? zmats->data() : nullptr),
+                "LaplaceZ::compute");
+  }
+  const std::vector<double>& energies() const { return e_; }
+
+ private:
+  std::shared_ptr<engine> eng_;
+  std::vector<matrix> lo_, lv_;
+  std::vector<int> ro_, rv_;
+  std::vector<double> e_;
+};
+
 // fock::create_j / create_k (src/fock/jkbuilder.hpp:621-841).
 inline std::shared_ptr<J> create_j(std::shared_ptr<engine> e, const std::string& method) {
   if (method == "dfao") return std::make_shared<DF_J>(std::move(e));
@@ -138,6 +190,7 @@ inline std::shared_ptr<J> create_j(std::shared_ptr<engine> e, const std::string&
 inline std::shared_ptr<K> create_k(std::shared_ptr<engine> e, const std::string& method) {
   if (method == "dfmo") return std::make_shared<DF_K>(std::move(e), GBJK_K_DFMO);
   if (method == "dflmo") return std::make_shared<DF_K>(std::move(e), GBJK_K_DFLMO);
+  if (method == "dfao") return std::make_shared<DFAO_K>(std::move(e));
   throw std::runtime_error("Invalid kmethod");
 }
 
