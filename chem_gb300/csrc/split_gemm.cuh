@@ -18,6 +18,8 @@
 // accumulate in FP32 over the whole k range (weights 2^-24 and 2^-32 of the
 // leading term) and are folded in with 16 fractional bits:
 //   value = 2^(eA+eB-46) (W 2^16 + rint(256 r3) + rint(r4)),
+// where each rint is taken as 32-bit halves with FP32 arithmetic (|256 r3|
+// stays below 2^38 for items of at most 8192 k), and the result is
 // assembled into an FP64 bit pattern with integer operations.
 //
 // Pipeline (one CTA per SM, persistent over a work list):
@@ -25,10 +27,12 @@
 //               images into a 3-stage shared-memory ring (mbarrier tx count)
 //   warp 1      TMEM allocation and the single MMA-issuing thread
 //   warps 2..13 epilogue: drain exact diagonals per chunk, write results
-// Per k-tile the MMA thread issues the exact-diagonal pairs first and commits
-// them, then the 9 approximate pairs (15 pairs as 9 MMAs of N = 96 or 192),
-// so the drain of chunk c overlaps the approximate MMAs.  Every wait is bounded (kSpinNs); on timeout the CTA
-// records an error code, drains its own copies and MMAs and frees TMEM.
+// Per k-tile the MMA thread issues the exact-diagonal pairs, commits them at
+// a chunk end, then the approximate pairs (15 pairs as 9 MMAs of N = 96 or
+// 192); at a chunk start it issues the approximate pairs first, so the drain
+// of chunk c overlaps the approximate MMAs of two k-tiles.  Every wait is
+// bounded (kSpinNs); on timeout the CTA records an error code, drains its
+// own copies and MMAs and frees TMEM.
 //
 // Shared-memory operand layout: K-major, no swizzle, 8x8 core matrices
 // (128 B); within a tile of R rows x 32 k the element (r, k) sits at byte
@@ -192,22 +196,16 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// rint(v * 2^k) for an FP32 value v, |v * 2^k| < 2^62, with integer
-// operations only (no 64-bit conversion instruction).
-__device__ __forceinline__ long long f32_scaled_rint(float v, int k) {
-  const unsigned int u = __float_as_uint(v);
-  const int E = (int)((u >> 23) & 0xFF);
-  if (E == 0) return 0;  // zero or subnormal (|v| < 2^-126)
-  const long long m = (long long)((u & 0x7FFFFF) | 0x800000);
-  const int sh = E - 150 + k;  // v * 2^k = m * 2^sh
-  long long r;
-  if (sh >= 0)
-    r = m << sh;
-  else if (sh > -25)
-    r = (m + (1ll << (-sh - 1))) >> (-sh);
-  else
-    r = 0;
-  return (u >> 31) ? -r : r;
+// rint(a) = h 2^16 + l for an FP32 value a with |a| < 2^38, in FP32
+// arithmetic only: h = rint(a 2^-16) by the 1.5*2^23 magic (a single fma
+// rounds a 2^-16 + magic), the remainder a - h 2^16 is exact (|.| <= 2^15),
+// and l = rint(remainder) by the same magic.  Ties round to even.
+__device__ __forceinline__ void f32_split16(float a, int& h, int& l) {
+  const float t = __fmaf_rn(a, 1.52587890625e-05f, 12582912.0f);
+  h = __float_as_int(t) - 0x4B400000;
+  const float hf = __fsub_rn(t, 12582912.0f);
+  const float r = __fmaf_rn(-hf, 65536.0f, a);
+  l = __float_as_int(__fadd_rn(r, 12582912.0f)) - 0x4B400000;
 }
 
 // v * 2^e2 rounded to nearest FP64, as a bit pattern built with integer
@@ -437,11 +435,6 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int k = 0; k < w.nkt && ok; ++k) {
           const bool chunk_start = (k % kChunkTiles) == 0;
           const bool chunk_end = ((k + 1) % kChunkTiles) == 0 || k + 1 == w.nkt;
-          if (chunk_start) {
-            ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4);
-            ex_phase ^= 1;
-            if (!ok) break;
-          }
           ok = mbar_wait(&full_bar[stage], phase, err, 5);
           if (!ok) break;
           tc_fence_after();
@@ -454,24 +447,44 @@ __global__ void __launch_bounds__(kThreads, 1)
           // adjacent accumulators, so one N = 192 MMA updates both.  Entries:
           // {s, t0, number of B slices, reset class}; reset class 1 = first
           // write of exact diagonals (reset at a chunk start), 2 = first write
-          // of d = 3, 4 (reset at the item's first k-tile).  The first four
-          // MMAs cover exactly the diagonals 0..2.
+          // of d = 3, 4 (reset at the item's first k-tile).  MMAs 0..3 cover
+          // exactly the diagonals 0..2, MMAs 4..8 the diagonals 3 and 4.
+          auto issue = [&](int q0, int q1) {
 #pragma unroll
-          for (int q = 0; q < 9; ++q) {
-            constexpr unsigned char qs[9] = {0, 0, 1, 2, 0, 1, 2, 3, 4};
-            constexpr unsigned char qt[9] = {0, 2, 0, 0, 3, 2, 1, 0, 0};
-            constexpr unsigned char qn[9] = {2, 1, 2, 1, 2, 2, 2, 2, 1};
-            constexpr unsigned char qr[9] = {1, 1, 0, 0, 2, 0, 0, 0, 0};
-            if (q == 4 && chunk_end) mma_commit(&exact_full);
-            const uint32_t dcol = tmem + (uint32_t)((qs[q] + qt[q]) * kTileN);
-            const uint32_t id = qn[q] == 2 ? idesc2 : idesc;
-            const bool reset = qr[q] == 1 ? chunk_start : (qr[q] == 2 ? k == 0 : false);
+            for (int q = 0; q < 9; ++q) {
+              constexpr unsigned char qs[9] = {0, 0, 1, 2, 0, 1, 2, 3, 4};
+              constexpr unsigned char qt[9] = {0, 2, 0, 0, 3, 2, 1, 0, 0};
+              constexpr unsigned char qn[9] = {2, 1, 2, 1, 2, 2, 2, 2, 1};
+              constexpr unsigned char qr[9] = {1, 1, 0, 0, 2, 0, 0, 0, 0};
+              if (q < q0 || q >= q1) continue;
+              const uint32_t dcol = tmem + (uint32_t)((qs[q] + qt[q]) * kTileN);
+              const uint32_t id = qn[q] == 2 ? idesc2 : idesc;
+              const bool reset = qr[q] == 1 ? chunk_start : (qr[q] == 2 ? k == 0 : false);
 #pragma unroll
-            for (int j = 0; j < 2; ++j) {
-              const uint64_t ad = adesc + (uint64_t)(qs[q] * kSliceA + j * 16);
-              const uint64_t bd = bdesc + (uint64_t)(qt[q] * kSliceB + j * 16);
-              mma_bf16(dcol, ad, bd, id, (reset && j == 0) ? 0u : 1u);
+              for (int j = 0; j < 2; ++j) {
+                const uint64_t ad = adesc + (uint64_t)(qs[q] * kSliceA + j * 16);
+                const uint64_t bd = bdesc + (uint64_t)(qt[q] * kSliceB + j * 16);
+                mma_bf16(dcol, ad, bd, id, (reset && j == 0) ? 0u : 1u);
+              }
             }
+          };
+          if (chunk_start) {
+            // d = 3, 4 first: they accumulate over the whole item and the
+            // exact drain does not read them, so they overlap the epilogue's
+            // drain of the previous chunk; the exact pairs wait for it
+            issue(4, 9);
+            ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4);
+            ex_phase ^= 1;
+            if (!ok) {
+              mma_commit(&empty_bar[stage]);  // the ring drain still completes
+              break;
+            }
+            issue(0, 4);
+            if (chunk_end) mma_commit(&exact_full);
+          } else {
+            issue(0, 4);
+            if (chunk_end) mma_commit(&exact_full);
+            issue(4, 9);
           }
           mma_commit(&empty_bar[stage]);
           if (++stage == kStages) {
@@ -539,9 +552,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         tmem_wait_ld();
 #pragma unroll
         for (int c = 0; c < 16; ++c) {
-          const long long r3 = f32_scaled_rint(__uint_as_float(v3[c]), 8);
-          const long long r4 = f32_scaled_rint(__uint_as_float(v4[c]), 0);
-          V[g * 16 + c] = (V[g * 16 + c] << 16) + r3 + r4;
+          int h3, l3, h4, l4;
+          f32_split16(__fmul_rn(__uint_as_float(v3[c]), 256.0f), h3, l3);
+          f32_split16(__uint_as_float(v4[c]), h4, l4);
+          V[g * 16 + c] = ((V[g * 16 + c] + (long long)(h3 + h4)) << 16) + (long long)(l3 + l4);
         }
       }
       // the accumulators are free for the next item before the stores
