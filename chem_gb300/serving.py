@@ -6,7 +6,9 @@ a J/K engine (its 3-center tensor, metric factors, digit slices and
 workspaces) and serves requests as they arrive:
 
 * set-up — the host integrals of a molecule not seen before run on a CPU
-  pipeline (one job at a time, each using all host threads);
+  pipeline (one job at a time, each using all host threads), shortest
+  estimated job first (a request's `cost` hint; arrival order without one),
+  except that a job waiting longer than `max_setup_wait` goes first;
 * admission — a molecule's engine is created when its device footprint fits
   the HBM budget; idle engines are evicted to make room, first those with
   no requests waiting (least-recently-used first), then any idle one;
@@ -30,7 +32,6 @@ import bisect
 import threading
 import time
 from collections import OrderedDict
-from concurrent.futures import ThreadPoolExecutor
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -42,6 +43,7 @@ class Request:
     key: str             # molecule identity
     arrival: float       # seconds after the start of the run
     make_system: object  # callable() -> (DFSystem, P_alpha, C_occ)
+    cost: float = None   # relative set-up cost estimate (shortest job first)
     t_setup_done: float = None
     t_admitted: float = None
     t_done: float = None
@@ -84,11 +86,12 @@ class FockServer:
 
     def __init__(self, budget_bytes=150e9, slots=4, precision="split", device=0,
                  engine_factory=None, clock=time.perf_counter, drop_host_tensor=True,
-                 max_host_bytes=48e9, progress=None):
+                 max_host_bytes=48e9, progress=None, max_setup_wait=60.0):
         self.budget = int(budget_bytes)
         self.drop_host_tensor = drop_host_tensor
         self.max_host_bytes = int(max_host_bytes)
         self.progress = progress  # callable(done, total) after each request
+        self.max_setup_wait = max_setup_wait
         self._host_pending = 0
         self._host_bytes = {}
         self.slots = slots
@@ -100,12 +103,14 @@ class FockServer:
         self._resident = OrderedDict()   # key -> _Resident (LRU order)
         self._used = 0
         self._systems = {}               # key -> (ds, P, C) once set up
-        self._setup_pending = {}         # key -> future
+        self._setup_waiters = {}         # key -> requests waiting for its set-up
+        self._setup_jobs = []            # (request, submit time) of pending set-ups
+        self._setup_done = set()         # keys set up (or failed)
+        self._submitted_all = False
         self._ready = []                 # sorted list of (arrival, rid, request)
         self._waiting = {}               # key -> requests submitted, not yet taken
         self._admitting = set()          # keys whose engine a slot is creating
         self._taken = 0
-        self._cpu = ThreadPoolExecutor(1)
         self.max_used = 0
         self.builds = 0
         self.log = []
@@ -281,32 +286,91 @@ class FockServer:
             if self.progress:
                 self.progress(done, total)
 
+    def _next_setup(self, now):
+        """Pick the next set-up job (caller holds _cv): the oldest one if it
+        has waited longer than max_setup_wait, else the cheapest."""
+        jobs = self._setup_jobs
+        i_old = min(range(len(jobs)), key=lambda i: jobs[i][1])
+        if now - jobs[i_old][1] > self.max_setup_wait:
+            return jobs.pop(i_old)[0]
+        i = min(range(len(jobs)), key=lambda i: (jobs[i][0].cost if jobs[i][0].cost is not None
+                                                 else 0.0, jobs[i][1]))
+        return jobs.pop(i)[0]
+
+    def _setup_loop(self, t0, total):
+        while True:
+            with self._cv:
+                while not self._setup_jobs and not self._submitted_all:
+                    self._cv.wait(0.05)
+                if not self._setup_jobs:
+                    return
+                req = self._next_setup(self.clock())
+            err = None
+            try:
+                self._setup(req)
+            except Exception as e:  # recorded on every request of the molecule
+                err = f"set-up failed: {e}"
+            with self._cv:
+                self._setup_done.add(req.key)
+                waiters = self._setup_waiters.pop(req.key, [])
+            for q in waiters:
+                if err is None:
+                    self._on_setup(q, t0)
+                else:
+                    self._fail(q, err, t0, total)
+
+    def _fail(self, req, err, t0, total):
+        req.error = err
+        req.t_done = self.clock() - t0
+        with self._cv:
+            self._waiting[req.key] -= 1
+            self._taken += 1
+            self._done += 1
+            done = self._done
+            self._cv.notify_all()
+        if self.progress:
+            self.progress(done, total)
+
+    def _submit(self, req, t0, total):
+        with self._cv:
+            if req.key in self._setup_done:
+                ok = req.key in self._systems
+            else:
+                first = req.key not in self._setup_waiters
+                self._setup_waiters.setdefault(req.key, []).append(req)
+                if first:
+                    self._setup_jobs.append((req, self.clock()))
+                    self._cv.notify_all()
+                return
+        if ok:
+            self._on_setup(req, t0)
+        else:
+            self._fail(req, "set-up failed earlier", t0, total)
+
     def run(self, requests, realtime=True):
         """Serve `requests` (arrival times relative to now); returns them."""
         reqs = sorted(requests, key=lambda q: q.arrival)
         self._done = 0
         self._taken = 0
+        self._submitted_all = False
         for q in reqs:
             self._waiting[q.key] = self._waiting.get(q.key, 0) + 1
         t0 = self.clock()
         workers = [threading.Thread(target=self._worker, args=(t0, len(reqs)), daemon=True)
                    for _ in range(self.slots)]
-        for w in workers:
+        setup = threading.Thread(target=self._setup_loop, args=(t0, len(reqs)), daemon=True)
+        for w in workers + [setup]:
             w.start()
-        futures = []
         for req in reqs:
             if realtime:
                 delay = req.arrival - (self.clock() - t0)
                 if delay > 0:
                     time.sleep(delay)
-            # set-up jobs run in arrival order on the CPU pipeline; later
-            # requests for the same molecule wait for the first one's job
-            fut = self._setup_pending.get(req.key)
-            if fut is None:
-                fut = self._cpu.submit(self._setup, req)
-                self._setup_pending[req.key] = fut
-            fut.add_done_callback(lambda _f, q=req: self._on_setup(q, t0))
-            futures.append(fut)
+            self._submit(req, t0, len(reqs))
+        with self._cv:
+            self._submitted_all = True
+            self._cv.notify_all()
+        setup.join()
         for w in workers:
             w.join()
         return reqs
@@ -317,7 +381,6 @@ class FockServer:
                 r.engine.close()
             self._resident.clear()
             self._used = 0
-        self._cpu.shutdown(wait=True)
 
 
 def latency_stats(requests):
@@ -365,5 +428,8 @@ def poisson_requests(n, rate, seed, alkane=(4, 40), water=(2, 32)):
         else:
             size = int(rng.integers(water[0], water[1] + 1))
             kind = "water"
-        out.append(Request(rid, f"{kind}{size}", t, make_system_factory(kind, size)))
+        # set-up cost grows ~ nbf^3 (3-center integrals with screening)
+        nbf = 24 * size + 10 if kind == "alkane" else 24 * size
+        out.append(Request(rid, f"{kind}{size}", t, make_system_factory(kind, size),
+                           cost=float(nbf) ** 3))
     return out

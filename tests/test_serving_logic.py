@@ -102,3 +102,32 @@ def test_no_double_admission_with_many_slots():
     srv.close()
     assert all(q.error is None for q in done)
     assert len(created) == 1
+
+
+def test_setup_runs_shortest_job_first_and_failures_do_not_hang():
+    order = []
+    ds = _DS(40, 200, 5)
+
+    def make(key, delay=0.02):
+        def f():
+            time.sleep(delay)
+            order.append(key)
+            if key == "bad":
+                raise ValueError("no basis")
+            return ds, np.eye(40), np.ones((40, 5))
+        return f
+
+    srv = FockServer(budget_bytes=10 * footprint_bytes(ds.layout, ds.nocc), slots=2,
+                     engine_factory=_FakeEngine)
+    reqs = [Request(0, "first", 0.0, make("first", 0.2), cost=0.5),
+            Request(1, "big", 0.0, make("big"), cost=9.0),
+            Request(2, "bad", 0.0, make("bad"), cost=1.0),
+            Request(3, "small", 0.0, make("small"), cost=2.0),
+            Request(4, "small", 0.0, make("small"), cost=2.0)]
+    done = srv.run(reqs, realtime=False)
+    srv.close()
+    # cheapest first, whatever the pipeline had queued when it started
+    assert order == ["first", "bad", "small", "big"]
+    assert done[2].error and "set-up failed" in done[2].error
+    assert all(q.error is None for q in done if q.key != "bad")
+    assert all(q.t_done is not None for q in done)
