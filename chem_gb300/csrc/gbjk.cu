@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "gbjk.h"
 #include "aok_host.cuh"
+#include "asymk_host.cuh"
 #include "kernels_fp64.cuh"
 #include "mp2_host.cuh"
 #include "split_host.cuh"
@@ -101,6 +102,8 @@ struct gbjk_ctx {
   Mp2State mp2;
   // DF-AO exchange (fitted coefficients, dense intermediates)
   AoKState aok;
+  // non-symmetric DF-LMO exchange (left and right coefficients)
+  AsymKState asymk;
   // profiling
   bool profile = false;
   cudaEvent_t ev[PH_COUNT][2] = {};
@@ -595,6 +598,7 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   ctx->mp2.release();
   ctx->aok.release();
+  ctx->asymk.release();
   ctx->split.release();
   void* ptrs[] = {ctx->d_blk_of, ctx->d_boff,  ctx->d_panelK, ctx->d_cmoff, ctx->d_colmap,
                   ctx->d_panel_off, ctx->d_pg_off, ctx->d_B, ctx->d_Linv, ctx->d_Vinv,
@@ -626,6 +630,7 @@ gbjk_status gbjk_upload_b(gbjk_ctx* ctx, const double* B) {
   ctx->ws_nocc = -1;  // plans hold d_B
   ctx->mp2.release();
   ctx->aok.release();
+  ctx->asymk.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -642,6 +647,7 @@ gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* 
   ctx->ws_nocc = -1;
   ctx->mp2.release();
   ctx->aok.release();
+  ctx->asymk.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -663,6 +669,7 @@ gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
   ctx->split.fitted = ctx->fitted;
   ctx->mp2.release();
   ctx->aok.release();
+  ctx->asymk.release();
   ctx->split.invalidate_b();
   ctx->ws_nocc = -1;  // exchange plan reads H or the fitted H
   return GBJK_OK;
@@ -673,6 +680,7 @@ gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows) {
   ctx->split.xb_req = rows;
   ctx->mp2.release();
   ctx->aok.release();
+  ctx->asymk.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -694,6 +702,7 @@ gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, doub
   ctx->ws_nocc = -1;
   ctx->mp2.release();
   ctx->aok.release();
+  ctx->asymk.release();
   ctx->split.invalidate_b();
   return GBJK_OK;
 }
@@ -897,7 +906,9 @@ gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int n
 }
 
 size_t gbjk_device_bytes(const gbjk_ctx* ctx) {
-  return ctx ? ctx->dev_bytes + ctx->split.bytes + ctx->mp2.bytes + ctx->aok.bytes : 0;
+  return ctx ? ctx->dev_bytes + ctx->split.bytes + ctx->mp2.bytes + ctx->aok.bytes +
+                   ctx->asymk.bytes
+             : 0;
 }
 int64_t gbjk_kernel_launches(const gbjk_ctx* ctx) { return ctx ? ctx->launches : 0; }
 
@@ -983,6 +994,45 @@ gbjk_status gbjk_compute_k_ao(gbjk_ctx* ctx, const double* P, double* K) {
   CK(cudaMemcpyAsync(ctx->d_P, P, n2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   if ((s = gbjk_compute_k_ao_dev(ctx, ctx->d_P, ctx->d_K))) return s;
   CK(cudaMemcpyAsync(K, ctx->d_K, n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  return gbjk_synchronize(ctx);
+}
+
+// --- non-symmetric DF-LMO exchange -----------------------------------------
+
+gbjk_status gbjk_compute_k_lmo_asym(gbjk_ctx* ctx, const double* U, const double* Vt, int nocc,
+                                    double* K) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (!U || !Vt || !K || nocc <= 0)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_compute_k_lmo_asym: null argument or nocc <= 0");
+  if (ctx->precision == GBJK_FP64 && ctx->fitted)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_compute_k_lmo_asym: FP64 path needs the metric");
+  if ((s = ensure_j_workspace(ctx))) return s;
+  if (ctx->precision == GBJK_SPLIT_BF16 && !ctx->split.b_ready &&
+      (s = ctx->split.prepare_b(ctx->stream, ctx->d_B, ctx->d_Linv, &ctx->launches, &ctx->err)))
+    return s;
+  AsymKState& a = ctx->asymk;
+  if (!a.ready || a.precision != ctx->precision || a.nocc != nocc) {
+    AsymKState::Layout L{ctx->nbf, ctx->naux, ctx->nblk, ctx->ncols_total, &ctx->bsize,
+                         &ctx->boff, &ctx->panelK, &ctx->cmoff, &ctx->panel_off};
+    if ((s = a.plan(ctx->precision, nocc, L, ctx->d_B, ctx->d_Vinv, ctx->split, &ctx->err)))
+      return s;
+  }
+  // v = Vt^T as nbf x nocc, row-major
+  const int nbf = ctx->nbf;
+  std::vector<double> v((size_t)nbf * nocc);
+  for (int i = 0; i < nocc; ++i)
+    for (int n = 0; n < nbf; ++n) v[(size_t)n * nocc + i] = Vt[(size_t)i * nbf + n];
+  CK(cudaMemcpyAsync(a.d_U, U, (size_t)nbf * nocc * 8, cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(a.d_V, v.data(), v.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  {
+    PhaseScope ps(ctx, PH_KGEMM);
+    if ((s = a.run(ctx->stream, nbf, ctx->naux, ctx->nblk, ctx->ncols_total, ctx->d_colmap,
+                   ctx->d_K, ctx->split, &ctx->launches, &ctx->err)))
+      return s;
+  }
+  if ((s = filter(ctx, ctx->d_K))) return s;
+  CK(cudaMemcpyAsync(K, ctx->d_K, (size_t)nbf * nbf * 8, cudaMemcpyDeviceToHost, ctx->stream));
   return gbjk_synchronize(ctx);
 }
 

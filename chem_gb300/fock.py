@@ -65,6 +65,7 @@ def lib():
         L.gbjk_compute_k.argtypes = [vp, C.c_int, dp, C.c_int, dp]
         L.gbjk_compute_jk.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, dp]
         L.gbjk_compute_k_ao.argtypes = [vp, dp, dp]
+        L.gbjk_compute_k_lmo_asym.argtypes = [vp, dp, dp, C.c_int, dp]
         L.gbjk_compute_k_ao_dev.argtypes = [vp, C.c_void_p, C.c_void_p]
         L.gbjk_compute_jk_dev.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                           C.c_void_p, C.c_void_p]
@@ -193,6 +194,18 @@ class JKEngine:
         P = np.ascontiguousarray(P, float)
         K = np.zeros((self.nbf, self.nbf))
         self._check(lib().gbjk_compute_k_ao(self.h, _dp(P), _dp(K)), "gbjk_compute_k_ao")
+        return K
+
+    def compute_k_lmo_asym(self, U, Vt):
+        """Non-symmetric DF-LMO K (gbjk_compute_k_lmo_asym): U nbf x nocc,
+        Vt nocc x nbf; K negated."""
+        U = np.ascontiguousarray(U, float)
+        Vt = np.ascontiguousarray(Vt, float)
+        if U.shape[0] != self.nbf or Vt.shape != (U.shape[1], self.nbf):
+            raise ValueError("U must be nbf x nocc and Vt nocc x nbf")
+        K = np.zeros((self.nbf, self.nbf))
+        self._check(lib().gbjk_compute_k_lmo_asym(self.h, _dp(U), _dp(Vt), U.shape[1], _dp(K)),
+                    "gbjk_compute_k_lmo_asym")
         return K
 
     def compute_k_ao_dev(self, dP, dK):
@@ -368,8 +381,24 @@ class DFMO_K(_DFK):
 
 
 class DFLMO_K(_DFK):
-    """fock::DFLMO_K, symmetric branch (src/fock/jkdf.cpp:861-1091)."""
+    """fock::DFLMO_K (src/fock/jkdf.cpp:861-1323): the symmetric branch from
+    set_coeff_alpha, or with set_sym(False) the non-symmetric one from
+    set_coeff_left_alpha (nbf x nocc) and set_coeff_right_alpha (nocc x nbf),
+    as the ADC matrix-vector products call it."""
     kmethod = "dflmo"
+
+    def set_coeff_left_alpha(self, U):
+        self.m_u_A = U
+
+    def set_coeff_right_alpha(self, Vt):
+        self.m_v_A = Vt
+
+    def compute_K(self):
+        if self.m_sym:
+            return super().compute_K()
+        if getattr(self, "m_u_A", None) is None or getattr(self, "m_v_A", None) is None:
+            raise RuntimeError("DFLMO_K: left/right coefficients not set")
+        self.m_K_A = self.engine.compute_k_lmo_asym(self.m_u_A, self.m_v_A)
 
 
 class DFAO_K(K):

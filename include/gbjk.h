@@ -128,6 +128,14 @@ gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int n
  * Host and device-pointer (stream-ordered) forms. */
 gbjk_status gbjk_compute_k_ao(gbjk_ctx* ctx, const double* P, double* K);
 gbjk_status gbjk_compute_k_ao_dev(gbjk_ctx* ctx, const double* dP, double* dK);
+/* Non-symmetric DF-LMO K (fock::DFLMO_K with set_sym(false),
+ * src/fock/jkdf.cpp:1093-1323; the exchange of the ADC matrix-vector
+ * products, set_coeff_left_alpha / set_coeff_right_alpha):
+ *   K_{mn} = -sum_{X,i} [(X|m.) U]_{Xmi} [V^-1 (X|n.) Vt^T]_{Xni},
+ * U: nbf x nocc (left), Vt: nocc x nbf (right, as the reference's v_mb).
+ * The split path uses the Cholesky route of the metric. */
+gbjk_status gbjk_compute_k_lmo_asym(gbjk_ctx* ctx, const double* U, const double* Vt, int nocc,
+                                    double* K);
 /* One Fock build: J from Ptot and K from Cocc in one call. */
 gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* Ptot, const double* Cocc,
                             int nocc, double* J, double* K);

@@ -129,6 +129,29 @@ class DF_K : public K {
   int kmethod_;
 };
 
+// fock::DFLMO_K with set_sym(false) (src/fock/jkdf.cpp:1093-1323): left
+// coefficients U (nbf x nocc) and right coefficients Vt (nocc x nbf), as
+// the ADC matrix-vector products set them.
+class DFLMO_K_asym : public K {
+ public:
+  using K::K;
+  void set_coeff_left_alpha(matrix u, int nocc) { m_u_A = std::move(u); m_nocc_u = nocc; }
+  void set_coeff_right_alpha(matrix vt) { m_vt_A = std::move(vt); }
+  void init() override {
+    m_K_A = std::make_shared<std::vector<double>>((size_t)eng_->nbf() * eng_->nbf());
+  }
+  void compute_K() override {
+    if (!m_u_A || !m_vt_A) throw std::runtime_error("DFLMO_K: left/right coefficients not set");
+    eng_->check(gbjk_compute_k_lmo_asym(eng_->ctx(), m_u_A->data(), m_vt_A->data(), m_nocc_u,
+                                        m_K_A->data()),
+                "DFLMO_K::compute_K");
+  }
+
+ private:
+  matrix m_u_A, m_vt_A;
+  int m_nocc_u = 0;
+};
+
 // fock::DFAO_K (src/fock/jkdf.cpp:464-648): K from the density with the
 // fitting coefficients V^-1 (X|mn) (src/ints/fitting.cpp:44-161).
 class DFAO_K : public K {

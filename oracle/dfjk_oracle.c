@@ -18,6 +18,10 @@
  *   oracle_dflmo_k   fock::DFLMO_K::compute_K   src/fock/jkdf.cpp:897-1091
  *                    (symmetric branch)
  *   oracle_dfao_k    fock::DFAO_K::compute_K    src/fock/jkdf.cpp:510-648
+ *   oracle_dflmo_k_asym  fock::DFLMO_K::compute_K, set_sym(false),
+ *                    src/fock/jkdf.cpp:1093-1323
+ *   oracle_prefit, oracle_mp2_ll_point  the SOS-AO-MP2 Laplace term
+ *                    (src/mp/z_full.cpp:427-620, src/mp/mp_compute.cpp:232-382)
  *   oracle_filter    dbcsr::tensor::filter / contract .filter(eps) applied to
  *                    the result matrix (src/dbcsrx/dbcsr_tensor.hpp:678-688)
  *
@@ -291,6 +295,28 @@ int oracle_dflmo_k(const oracle_layout* L, const double* B, const double* Vinv, 
   contract_k(L, Hf, H, nocc, K, 0, kchunk);
   oracle_filter(L, K, eps);
   free(H);
+  free(Hf);
+  return 0;
+}
+
+/* DF-LMO K, non-symmetric branch (jkdf.cpp:1093-1323): HTu = B U,
+ * HTv = B V (V = Vt^T, nbf x nocc), HTvfit = V^-1 HTv,
+ * K_mn = -sum_{X,i} HTu[m][X][i] HTvfit[n][X][i]. */
+int oracle_dflmo_k_asym(const oracle_layout* L, const double* B, const double* Vinv,
+                        const double* U, const double* V, int nocc, double* K, double eps,
+                        long long kchunk) {
+  const size_t sz = (size_t)L->nbf * L->naux * nocc;
+  double* Hu = (double*)malloc(sizeof(double) * sz);
+  double* Hv = (double*)malloc(sizeof(double) * sz);
+  double* Hf = (double*)malloc(sizeof(double) * sz);
+  if (!Hu || !Hv || !Hf) { free(Hu); free(Hv); free(Hf); return 2; }
+  oracle_half_transform(L, B, U, nocc, Hu);
+  oracle_half_transform(L, B, V, nocc, Hv);
+  apply_metric(L, Vinv, 0, Hv, nocc, Hf);
+  contract_k(L, Hu, Hf, nocc, K, 0, kchunk);
+  oracle_filter(L, K, eps);
+  free(Hu);
+  free(Hv);
   free(Hf);
   return 0;
 }

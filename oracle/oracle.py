@@ -57,6 +57,8 @@ def lib():
         L.oracle_half_transform.argtypes = [lp, dp, dp, C.c_int, dp]
         L.oracle_filter.argtypes = [lp, dp, C.c_double]
         L.oracle_prefit.argtypes = [lp, dp, dp, C.c_int, dp]
+        L.oracle_dflmo_k_asym.argtypes = [lp, dp, dp, dp, dp, C.c_int, dp, C.c_double,
+                                          C.c_longlong]
         L.oracle_mp2_ll_point.argtypes = [lp, dp, dp, C.c_int, dp, C.c_int, C.c_longlong,
                                           C.c_int, dp, dp]
         _lib = L
@@ -134,6 +136,19 @@ class Oracle:
                                  _dp(np.ascontiguousarray(P)), _dp(K), eps, int(kchunk))
         if rc:
             raise MemoryError("oracle_dfao_k")
+        return K
+
+    def dflmo_k_asym(self, Vinv, U, Vt, eps=0.0, kchunk=0):
+        """Non-symmetric DF-LMO K from left U (nbf x nocc) and right Vt
+        (nocc x nbf) coefficients."""
+        n = self.layout.nbf
+        K = np.zeros((n, n))
+        U = np.ascontiguousarray(U, float)
+        V = np.ascontiguousarray(np.asarray(Vt, float).T)
+        rc = lib().oracle_dflmo_k_asym(C.byref(self.L), _dp(self.B), _dp(np.ascontiguousarray(Vinv)),
+                                       _dp(U), _dp(V), U.shape[1], _dp(K), eps, int(kchunk))
+        if rc:
+            raise MemoryError("oracle_dflmo_k_asym")
         return K
 
     def half_transform(self, Cocc):
@@ -234,3 +249,10 @@ def dense_sos_mp2(T, Vinv, C_occ, C_vir, e_occ, e_vir):
     den = (e_vir[None, :, None, None] + e_vir[None, None, None, :]
            - e_occ[:, None, None, None] - e_occ[None, None, :, None])
     return float(np.sum(iajb ** 2 / den))
+
+
+def dense_dflmo_k_asym(T, Vinv, U, Vt):
+    Hu = np.einsum("xmn,ni->xmi", T, U)
+    Hv = np.einsum("xmn,in->xmi", T, Vt)
+    Hf = np.einsum("xy,ymi->xmi", Vinv, Hv)
+    return -np.einsum("xmi,xni->mn", Hu, Hf)

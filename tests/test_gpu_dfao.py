@@ -66,3 +66,42 @@ def test_dfao_builder_interface(water):
     assert np.abs(k.get_K_A() - Kmo).max() <= 1e-9
     assert k.get_K_B() is None
     eng.close()
+
+
+@pytest.mark.parametrize("sysname", ["water", "decane"])
+def test_dflmo_asym_fp64_bitwise_and_split(sysname, request):
+    """Non-symmetric DF-LMO K (ADC-style left/right coefficients)."""
+    from chem_gb300.fock import k_split_plan
+    from oracle.oracle import Oracle
+    ds = request.getfixturevalue(sysname)
+    rng = np.random.default_rng(9)
+    C, _ = _density(ds)
+    U = C + 0.1 * rng.standard_normal(C.shape)
+    Vt = (C + 0.1 * rng.standard_normal(C.shape)).T.copy()
+    e64 = _engine(ds, "fp64")
+    K64 = e64.compute_k_lmo_asym(U, Vt)
+    e64.close()
+    kc = k_split_plan(ds.nbf, ds.naux, U.shape[1])[1]
+    Kr = Oracle(ds.layout, ds.B).dflmo_k_asym(ds.Vinv, U, Vt, 0.0, kchunk=kc)
+    assert np.array_equal(K64, Kr), np.abs(K64 - Kr).max()
+    es = _engine(ds, "split")
+    Ks = es.compute_k_lmo_asym(U, Vt)
+    es.close()
+    assert np.abs(Ks - K64).max() <= 1e-9 * max(1.0, np.abs(K64).max())
+    assert np.abs(K64 - K64.T).max() > 1e-6  # genuinely non-symmetric
+
+
+def test_dflmo_builder_nonsymmetric(water):
+    from chem_gb300.fock import create_k
+    ds = water
+    C, _ = _density(ds)
+    eng = _engine(ds, "split")
+    k = create_k(eng, "dflmo")
+    k.init()
+    k.set_sym(False)
+    k.set_coeff_left_alpha(C)
+    k.set_coeff_right_alpha(C.T)
+    k.compute_K()
+    _, Kmo = eng.compute_jk(Cocc=C)
+    assert np.abs(k.get_K_A() - Kmo).max() <= 1e-9
+    eng.close()

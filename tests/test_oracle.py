@@ -75,3 +75,21 @@ def test_layout_screening(butane):
         for J in L.nbr[I]:
             assert I in L.nbr[J]
     assert L.nnz == sum(int(L.bsizes[I]) * L.naux * int(L.panel_K[I]) for I in range(L.nblk))
+
+
+def test_dflmo_asym_oracle_matches_dense(water):
+    import numpy as np
+    from oracle.oracle import Oracle, dense_dflmo_k_asym
+    ds = water
+    rng = np.random.default_rng(5)
+    U = rng.standard_normal((ds.nbf, 4))
+    Vt = rng.standard_normal((4, ds.nbf))
+    T = ds.layout.to_dense(ds.B)
+    K = Oracle(ds.layout, ds.B).dflmo_k_asym(ds.Vinv, U, Vt)
+    Kd = dense_dflmo_k_asym(T, ds.Vinv, U, Vt)
+    assert np.abs(K - Kd).max() < 1e-11 * np.abs(Kd).max()
+    # U = V gives the symmetric branch's K (which is stored as K_nm, so its
+    # transpose matches operation for operation)
+    Ks = Oracle(ds.layout, ds.B).dflmo_k(ds.Vinv, U)
+    Ka = Oracle(ds.layout, ds.B).dflmo_k_asym(ds.Vinv, U, U.T)
+    assert np.array_equal(Ks.T, Ka)
