@@ -40,9 +40,11 @@ def test_ragged_panels_and_single_orbital(h2_far):
         es.close()
         assert np.abs(Ks - K).max() <= 1e-10
         assert np.abs(Js - J).max() <= 1e-8
-        # screened block pairs stay exact zeros in both paths
+        # J of a screened block pair is an exact zero in both paths (K is
+        # not: delocalised orbitals couple the two molecules)
         bo = ds.layout.boff
-        assert not K[bo[0]:bo[1], bo[2]:bo[3]].any() and not Ks[bo[0]:bo[1], bo[2]:bo[3]].any()
+        assert not J[bo[0]:bo[1], bo[2]:bo[3]].any() and not Js[bo[0]:bo[1], bo[2]:bo[3]].any()
+        assert np.abs(K[bo[0]:bo[1], bo[2]:bo[3]]).max() > 1e-6
 
 
 def test_engine_reuse_across_nocc(water):
