@@ -77,10 +77,10 @@ struct gbjk_ctx {
   double *d_Linv = nullptr, *d_Vinv = nullptr;
   bool have_B = false, have_metric = false;
   bool fitted = false;  // the uploaded tensor already is L^-1 B (no metric)
-  bool colsum_smem_set = false, colsum2_smem_set = false;
+  bool colsum_smem_set = false;
   // J workspace
   double *d_P = nullptr, *d_Pg = nullptr, *d_part = nullptr, *d_g = nullptr, *d_h = nullptr,
-         *d_y = nullptr, *d_J = nullptr;
+         *d_y = nullptr, *d_J = nullptr, *d_jpart = nullptr;
   int jmode = GBJK_J_VINV;
   // K workspace (per nocc)
   int ws_nocc = -1;
@@ -214,6 +214,8 @@ void resolve_profile(gbjk_ctx* ctx) {
 }
 
 int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
+// auxiliary rows per block of the mixed-path J column sums
+constexpr int kColsumChunk = 512;
 
 void add_tiles(std::vector<GemmTile>& tiles, int group, int M, int N, int k0, int k1,
                long long coff, bool upper_only) {
@@ -382,6 +384,9 @@ gbjk_status ensure_j_workspace(gbjk_ctx* ctx) {
   if ((s = dalloc(ctx, &ctx->d_y, naux))) return s;
   if ((s = dalloc(ctx, &ctx->d_J, nbf * nbf))) return s;
   if ((s = dalloc(ctx, &ctx->d_K, nbf * nbf))) return s;
+  if ((s = dalloc(ctx, &ctx->d_jpart,
+                  (size_t)cdiv(naux, kColsumChunk) * nbf * std::max(1, ctx->maxK))))
+    return s;
   return GBJK_OK;
 }
 
@@ -603,6 +608,7 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   void* ptrs[] = {ctx->d_blk_of, ctx->d_boff,  ctx->d_panelK, ctx->d_cmoff, ctx->d_colmap,
                   ctx->d_panel_off, ctx->d_pg_off, ctx->d_B, ctx->d_Linv, ctx->d_Vinv,
                   ctx->d_P, ctx->d_Pg, ctx->d_part, ctx->d_g, ctx->d_h, ctx->d_y, ctx->d_J,
+                  ctx->d_jpart,
                   ctx->d_C, ctx->d_Cg, ctx->d_H, ctx->d_H2, ctx->d_Kpart, ctx->d_K,
                   ctx->d_groups, ctx->d_tiles};
   for (void* p : ptrs)
@@ -774,15 +780,15 @@ static gbjk_status run_jk_split(gbjk_ctx* ctx, const double* dP, const double* d
   }
   {
     PhaseScope ps(ctx, PH_J_COLSUM);
-    const size_t hbytes = (size_t)naux * sizeof(float2);
-    if (hbytes > 48 * 1024 && !ctx->colsum2_smem_set) {
-      CK(cudaFuncSetAttribute(k_j_colsum_f32x2, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)hbytes));
-      ctx->colsum2_smem_set = true;
-    }
-    k_j_colsum_f32x2<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, hbytes, ctx->stream>>>(
-        ctx->split.Bfit, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK,
-        ctx->d_cmoff, ctx->d_colmap, ctx->split.d_dt, nbf, naux, dJ);
+    const int xchunk = kColsumChunk, nchunk = cdiv(naux, xchunk);
+    k_j_colsum_f32x2<<<dim3(cdiv(ctx->maxK, 128), nbf, nchunk), 128, xchunk * sizeof(float2),
+                       ctx->stream>>>(ctx->split.Bfit, ctx->d_panel_off, ctx->d_blk_of,
+                                      ctx->d_boff, ctx->d_panelK, ctx->split.d_dt, nbf, naux,
+                                      xchunk, ctx->maxK, ctx->d_jpart);
+    k_j_colsum_chunks<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, 0, ctx->stream>>>(
+        ctx->d_jpart, nchunk, nbf, ctx->maxK, ctx->d_blk_of, ctx->d_panelK, ctx->d_cmoff,
+        ctx->d_colmap, dJ);
+    ctx->launches++;
     CKL(PH_J_COLSUM);
   }
   return filter(ctx, dJ);

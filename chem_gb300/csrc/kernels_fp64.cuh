@@ -166,17 +166,23 @@ __device__ __forceinline__ void f64_split_f32(double x, float& hi, float& lo) {
 // products and the sum in FP32 pairs (hi/lo operands, exact product error
 // by fma, TwoSum accumulation): about 46 significant bits, no FP64
 // arithmetic in the loop, so the pass runs at HBM speed rather than at
-// GB300's FP64 rate.  grid (ceil(maxK/128), nbf), dynamic smem naux float2.
+// GB300's FP64 rate.  The auxiliary range is cut into chunks of xchunk rows
+// (blockIdx.z) so that the grid is several waves deep; chunk z writes its
+// partial column sums to part[(z * nbf + mu) * maxK + k] and
+// k_j_colsum_chunks adds the chunks in order.
+// grid (ceil(maxK/128), nbf, nchunk), dynamic smem xchunk float2.
 __global__ void k_j_colsum_f32x2(const double* __restrict__ B,
                                  const long long* __restrict__ panel_off,
                                  const int* __restrict__ blk_of, const int* __restrict__ boff,
-                                 const int* __restrict__ panel_K, const int* __restrict__ cmoff,
-                                 const int* __restrict__ colmap, const double* __restrict__ h,
-                                 int nbf, int naux, double* __restrict__ J) {
+                                 const int* __restrict__ panel_K, const double* __restrict__ h,
+                                 int nbf, int naux, int xchunk, int maxK,
+                                 double* __restrict__ part) {
   extern __shared__ float2 h2[];
-  for (int x = threadIdx.x; x < naux; x += blockDim.x) {
+  const int x0 = blockIdx.z * xchunk;
+  const int nx = min(xchunk, naux - x0);
+  for (int x = threadIdx.x; x < nx; x += blockDim.x) {
     float a, b;
-    f64_split_f32(h[x], a, b);
+    f64_split_f32(h[x0 + x], a, b);
     h2[x] = make_float2(a, b);
   }
   __syncthreads();
@@ -186,7 +192,8 @@ __global__ void k_j_colsum_f32x2(const double* __restrict__ B,
   const int KI = panel_K[I];
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= KI) return;
-  const double* bp = B + panel_off[I] + (long long)m * naux * KI + k;
+  const double* bp = B + panel_off[I] + ((long long)m * naux + x0) * KI + k;
+  const int naux_ = nx;  // rows of this chunk
   float sh0 = 0.f, sl0 = 0.f, se0 = 0.f, sh1 = 0.f, sl1 = 0.f, se1 = 0.f;
   // explicit round-to-nearest intrinsics: no multiply-add contraction may
   // merge the product into the TwoSum
@@ -203,7 +210,7 @@ __global__ void k_j_colsum_f32x2(const double* __restrict__ B,
   };
   int X = 0;
   // eight loads in flight per thread
-  for (; X + 7 < naux; X += 8) {
+  for (; X + 7 < naux_; X += 8) {
     double v[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) v[j] = __ldg(bp + (long long)(X + j) * KI);
@@ -216,20 +223,35 @@ __global__ void k_j_colsum_f32x2(const double* __restrict__ B,
       acc(b1h, b1l, h2[X + j + 1], sh1, sl1, se1);
     }
   }
-  for (; X + 1 < naux; X += 2) {
+  for (; X + 1 < naux_; X += 2) {
     float b0h, b0l, b1h, b1l;
     f64_split_f32(bp[(long long)X * KI], b0h, b0l);
     f64_split_f32(bp[(long long)(X + 1) * KI], b1h, b1l);
     acc(b0h, b0l, h2[X], sh0, sl0, se0);
     acc(b1h, b1l, h2[X + 1], sh1, sl1, se1);
   }
-  if (X < naux) {
+  if (X < naux_) {
     float bh, bl;
     f64_split_f32(bp[(long long)X * KI], bh, bl);
     acc(bh, bl, h2[X], sh0, sl0, se0);
   }
   const double s = ((double)sh0 + (double)sh1) + (((double)sl0 + (double)sl1) +
                                                    ((double)se0 + (double)se1));
+  part[((long long)blockIdx.z * nbf + mu) * maxK + k] = s;
+}
+
+// J[mu][colmap(k)] = sum over chunks (in order) of part[z][mu][k].
+// grid (ceil(maxK/128), nbf).
+__global__ void k_j_colsum_chunks(const double* __restrict__ part, int nchunk, int nbf, int maxK,
+                                  const int* __restrict__ blk_of, const int* __restrict__ panel_K,
+                                  const int* __restrict__ cmoff, const int* __restrict__ colmap,
+                                  double* __restrict__ J) {
+  const int mu = blockIdx.y;
+  const int I = blk_of[mu];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= panel_K[I]) return;
+  double s = 0.0;
+  for (int z = 0; z < nchunk; ++z) s += part[((long long)z * nbf + mu) * maxK + k];
   J[(long long)mu * nbf + colmap[cmoff[I] + k]] = s;
 }
 
