@@ -1,0 +1,368 @@
+// 3-center Coulomb integrals (X|mu nu) on the device, written straight into
+// the atom-block panel layout of the resident tensor.
+//
+// The host engine (chem_gb300/csrc/ints, standing in for the libcint calls
+// of megalochem's ints::aoloader, src/ints/integrals.cpp:250-370) computes
+// the same tensor; this kernel follows its McMurchie-Davidson scheme and
+// conventions (normalised contractions exported by gbints_basis_shells,
+// real spherical harmonics from gbints_sph_coeffs, the primitive cut 1e-16)
+// so that the two agree to rounding:
+//   for a primitive pair (a_i, b_j): Hermite coefficients E^{ab}_{tuv}
+//   (Helgaker, Jorgensen, Olsen eq. 9.5.6-9.5.7), for every auxiliary
+//   primitive c_k the Hermite Coulomb integrals R_{tuv}(alpha, P - C)
+//   (eq. 9.9.18-9.9.20, Boys function by its series and downward recursion,
+//   or erf and upward recursion for large arguments), contracted with the
+//   single-centre expansion of c and its spherical transform into
+//   W[tuv][mc], then with E^{ab} into the cartesian (a, b) accumulators,
+//   and finally transformed to spherical (a, b).
+// Work: one block per AO shell pair (a in block I, b in block J, a <= b
+// when I == J) of a kept block pair; its 4 warps take the auxiliary shells
+// of the kept auxiliary blocks in turn.  Lanes split the Hermite indices of
+// the bra (W) and the cartesian pairs (accumulators); the R table of a
+// primitive triple lives in the warp's shared memory.  Supported: AO shells
+// up to d and auxiliary shells up to f (la + lb + lc <= 7); the host checks.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gbjk {
+
+constexpr int kEriMaxLao = 2, kEriMaxLaux = 3;
+constexpr int kEriMaxL = 2 * kEriMaxLao + kEriMaxLaux;                           // 7
+constexpr int kEriNR = (kEriMaxL + 1) * (kEriMaxL + 2) * (kEriMaxL + 3) / 6;     // 120
+constexpr int kEriLb = 2 * kEriMaxLao;                                           // 4
+constexpr int kEriNW = (kEriLb + 1) * (kEriLb + 2) * (kEriLb + 3) / 6;           // 35
+constexpr int kEriNcab = 36;  // (d cartesians)^2
+constexpr int kEriMaxSph = 7;
+constexpr int kEriWarps = 4;
+constexpr int kEriWarpDoubles = 2 * kEriNR + kEriNW * kEriMaxSph + 16;  // R x2, W, rn
+// cartesian -> spherical tables for l = 0..3, at offsets 0, 1, 10, 40
+__constant__ double c_eri_sph[1 + 9 + 30 + 70];
+
+struct EriShell {
+  int l, nprim, prim0, bf_off;
+  double A[3];
+};
+struct EriItem {
+  int p, a, b;
+};
+
+__device__ __forceinline__ int eri_tet(int n) { return n * (n + 1) * (n + 2) / 6; }
+// compact index of (t, u, v) among all t + u + v <= L (independent of L)
+__device__ __forceinline__ int eri_idx(int t, int u, int v) {
+  const int s = t + u + v, r = u + v;
+  return eri_tet(s) + r * (r + 1) / 2 + v;
+}
+__device__ __forceinline__ int eri_sph_off(int l) { return l == 0 ? 0 : l == 1 ? 1 : l == 2 ? 10 : 40; }
+__device__ __forceinline__ void eri_cart(int l, int c, int* ex) {
+  int idx = 0;
+  for (int ix = l; ix >= 0; --ix)
+    for (int iy = l - ix; iy >= 0; --iy) {
+      if (idx == c) {
+        ex[0] = ix;
+        ex[1] = iy;
+        ex[2] = l - ix - iy;
+        return;
+      }
+      ++idx;
+    }
+}
+
+// Boys function F_0..F_n at T (same algorithm as the host engine).
+__device__ void eri_boys(int nmax, double T, double* F) {
+  if (T < 1e-15) {
+    for (int m = 0; m <= nmax; ++m) F[m] = 1.0 / (2 * m + 1);
+    return;
+  }
+  const double eT = exp(-T);
+  if (T > 33.0 + nmax) {
+    F[0] = 0.5 * sqrt(3.14159265358979323846 / T) * erf(sqrt(T));
+    const double inv2T = 0.5 / T;
+    for (int m = 0; m < nmax; ++m) F[m + 1] = ((2 * m + 1) * F[m] - eT) * inv2T;
+    return;
+  }
+  double denom = 2 * nmax + 1;
+  double term = 1.0 / denom;
+  double sum = term;
+  const double twoT = 2.0 * T;
+  for (int k = 1; k < 400; ++k) {
+    denom += 2.0;
+    term *= twoT / denom;
+    sum += term;
+    if (term < 1e-17 * sum) break;
+  }
+  F[nmax] = eT * sum;
+  for (int m = nmax - 1; m >= 0; --m) F[m] = (twoT * F[m + 1] + eT) / (2 * m + 1);
+}
+
+// E[axis][i][j][t] of one primitive pair, i <= la, j <= lb, t <= i + j, in
+// a flat array with strides ((lb+1)*(la+lb+1), (la+lb+1), 1) per axis.
+__device__ void eri_hermite_pair(int la, int lb, double p, const double* PA, const double* PB,
+                                 double kab, double* E) {
+  const int nt = la + lb + 1, sj = nt, si = (lb + 1) * nt, sax = (la + 1) * si;
+  const double oo2p = 0.5 / p;
+  for (int d = 0; d < 3; ++d) {
+    double* e = E + d * sax;
+    for (int i = 0; i < sax; ++i) e[i] = 0.0;
+    e[0] = d == 0 ? kab : 1.0;
+    for (int i = 0; i < la; ++i)
+      for (int t = 0; t <= i + 1; ++t) {
+        double v = PA[d] * e[i * si + t] + (t + 1 < nt ? (t + 1) * e[i * si + t + 1] : 0.0);
+        if (t > 0) v += oo2p * e[i * si + t - 1];
+        e[(i + 1) * si + t] = v;
+      }
+    for (int i = 0; i <= la; ++i)
+      for (int j = 0; j < lb; ++j)
+        for (int t = 0; t <= i + j + 1; ++t) {
+          double v = PB[d] * e[i * si + j * sj + t] +
+                     (t + 1 < nt ? (t + 1) * e[i * si + j * sj + t + 1] : 0.0);
+          if (t > 0) v += oo2p * e[i * si + j * sj + t - 1];
+          e[i * si + (j + 1) * sj + t] = v;
+        }
+  }
+}
+
+__global__ void __launch_bounds__(32 * kEriWarps)
+    k_eri3c(const EriItem* __restrict__ items, const EriShell* __restrict__ ao,
+            const EriShell* __restrict__ ax, const double* __restrict__ ao_alpha,
+            const double* __restrict__ ao_coef, const double* __restrict__ ax_alpha,
+            const double* __restrict__ ax_coef, const int* __restrict__ pair_I,
+            const int* __restrict__ pair_J, const unsigned char* __restrict__ keep, int nablk,
+            const int* __restrict__ ablk_shell_off, const int* __restrict__ blk_bf_off,
+            const long long* __restrict__ panel_off, const int* __restrict__ panel_K,
+            const int* __restrict__ col_IJ, const int* __restrict__ col_JI, int naux,
+            double* __restrict__ B) {
+  extern __shared__ double sm[];
+  const EriItem it = items[blockIdx.x];
+  const EriShell a = ao[it.a], b = ao[it.b];
+  const int la = a.l, lb = b.l, Lb = la + lb;
+  const int nca = (la + 1) * (la + 2) / 2, ncb = (lb + 1) * (lb + 2) / 2;
+  const int nsa = 2 * la + 1, nsb = 2 * lb + 1;
+  const int npp = a.nprim * b.nprim;
+  const int esz = 3 * (la + 1) * (lb + 1) * (Lb + 1);  // E doubles per primitive pair
+  const int psz = 6 + esz;                              // p, P[3], coef, keep flag, E
+  const int nW = eri_tet(Lb + 1);                       // bra Hermite indices
+  double* pp = sm;                                      // npp * psz
+  double* wbase = sm + npp * psz + (threadIdx.x >> 5) * kEriWarpDoubles;
+  double* R0 = wbase;
+  double* R1 = wbase + kEriNR;
+  double* W = wbase + 2 * kEriNR;
+  double* rn = W + kEriNW * kEriMaxSph;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+  // bra primitive pairs
+  double ab2 = 0.0;
+  for (int d = 0; d < 3; ++d) ab2 += (a.A[d] - b.A[d]) * (a.A[d] - b.A[d]);
+  for (int q = threadIdx.x; q < npp; q += blockDim.x) {
+    const int ia = q / b.nprim, ib = q % b.nprim;
+    const double al = ao_alpha[a.prim0 + ia], be = ao_alpha[b.prim0 + ib];
+    const double p = al + be;
+    double P[3], PA[3], PB[3];
+    for (int d = 0; d < 3; ++d) {
+      P[d] = (al * a.A[d] + be * b.A[d]) / p;
+      PA[d] = P[d] - a.A[d];
+      PB[d] = P[d] - b.A[d];
+    }
+    const double kab = exp(-al * be / p * ab2);
+    const double coef = ao_coef[a.prim0 + ia] * ao_coef[b.prim0 + ib];
+    double* o = pp + q * psz;
+    o[0] = p;
+    o[1] = P[0];
+    o[2] = P[1];
+    o[3] = P[2];
+    o[4] = coef;
+    o[5] = fabs(coef * kab) < 1e-16 ? 0.0 : 1.0;
+    eri_hermite_pair(la, lb, p, PA, PB, kab, o + 6);
+  }
+  __syncthreads();
+
+  const int I = pair_I[it.p], J = pair_J[it.p];
+  const int Eax = (la + 1) * (lb + 1) * (Lb + 1), Esi = (lb + 1) * (Lb + 1), Esj = Lb + 1;
+  // shells of the kept auxiliary blocks, in turn over the warps
+  int counter = 0;
+  for (int A = 0; A < nablk; ++A) {
+    if (!keep[(long long)it.p * nablk + A]) continue;
+    for (int s = ablk_shell_off[A]; s < ablk_shell_off[A + 1]; ++s, ++counter) {
+      if (counter % kEriWarps != warp) continue;
+      const EriShell c = ax[s];
+      const int lc = c.l, ncc = (lc + 1) * (lc + 2) / 2, nsc = 2 * lc + 1;
+      const int L = Lb + lc;
+      const double* sc = c_eri_sph + eri_sph_off(lc);
+      double acc0[kEriMaxSph], acc1[kEriMaxSph];  // cartesian pairs lane, lane + 32
+      for (int m = 0; m < kEriMaxSph; ++m) acc0[m] = acc1[m] = 0.0;
+      for (int q = 0; q < npp; ++q) {
+        const double* o = pp + q * psz;
+        if (o[5] == 0.0) continue;
+        const double p = o[0];
+        double w0[kEriMaxSph], w1[kEriMaxSph];  // W for bra indices lane, lane + 32
+        for (int m = 0; m < kEriMaxSph; ++m) w0[m] = w1[m] = 0.0;
+        for (int k = 0; k < c.nprim; ++k) {
+          const double qq = ax_alpha[c.prim0 + k];
+          const double alpha = p * qq / (p + qq);
+          const double pref = 2.0 * 17.493418327624862 / (p * qq * sqrt(p + qq)) * o[4] *
+                              ax_coef[c.prim0 + k];  // 2 pi^{5/2}
+          const double X = o[1] - c.A[0], Y = o[2] - c.A[1], Z = o[3] - c.A[2];
+          if (lane == 0) {
+            double F[kEriMaxL + 1];
+            eri_boys(L, alpha * (X * X + Y * Y + Z * Z), F);
+            double fac = 1.0;
+            for (int n = 0; n <= L; ++n) {
+              rn[n] = fac * F[n];
+              fac *= -2.0 * alpha;
+            }
+          }
+          __syncwarp();
+          // R^n_{tuv}, levels n = L .. 0; level 0 ends in Rc
+          double* cur = (L & 1) ? R1 : R0;
+          double* old = (L & 1) ? R0 : R1;
+          if (lane == 0) cur[0] = rn[L];
+          __syncwarp();
+          for (int n = L - 1; n >= 0; --n) {
+            double* t_ = cur;
+            cur = old;
+            old = t_;
+            const int lt = L - n, cnt = eri_tet(lt + 1);
+            for (int e = lane; e < cnt; e += 32) {
+              // decode e -> (t, u, v), t + u + v <= lt
+              int sidx = 0;
+              while (eri_tet(sidx + 1) <= e) ++sidx;
+              int rem = e - eri_tet(sidx), r = 0;
+              while ((r + 1) * (r + 2) / 2 <= rem) ++r;
+              const int v = rem - r * (r + 1) / 2, u = r - v, t = sidx - r;
+              double val;
+              if (t > 0) {
+                val = X * old[eri_idx(t - 1, u, v)];
+                if (t > 1) val += (t - 1) * old[eri_idx(t - 2, u, v)];
+              } else if (u > 0) {
+                val = Y * old[eri_idx(t, u - 1, v)];
+                if (u > 1) val += (u - 1) * old[eri_idx(t, u - 2, v)];
+              } else if (v > 0) {
+                val = Z * old[eri_idx(t, u, v - 1)];
+                if (v > 1) val += (v - 1) * old[eri_idx(t, u, v - 2)];
+              } else {
+                val = rn[n];
+              }
+              cur[e] = val;
+            }
+            __syncwarp();
+          }
+          const double* Rc = cur;
+          // single-centre Hermite expansion of c: Ec[i][t], i <= lc
+          double Ec[4][4];
+          for (int i = 0; i < 4; ++i)
+            for (int t = 0; t < 4; ++t) Ec[i][t] = 0.0;
+          Ec[0][0] = 1.0;
+          const double oo2q = 0.5 / qq;
+          for (int i = 0; i < lc; ++i)
+            for (int t = 0; t <= i + 1; ++t) {
+              double v = (t + 1 <= 3 ? (t + 1) * Ec[i][t + 1] : 0.0);
+              if (t > 0) v += oo2q * Ec[i][t - 1];
+              Ec[i + 1][t] = v;
+            }
+          // W[tuv][mc] += pref sum_cc sph[mc][cc] sum_ket sign E R
+          for (int h = 0; h < 2; ++h) {
+            const int e = lane + 32 * h;
+            if (e >= nW) break;
+            int sidx = 0;
+            while (eri_tet(sidx + 1) <= e) ++sidx;
+            int rem = e - eri_tet(sidx), r = 0;
+            while ((r + 1) * (r + 2) / 2 <= rem) ++r;
+            const int v = rem - r * (r + 1) / 2, u = r - v, t = sidx - r;
+            for (int cc = 0; cc < ncc; ++cc) {
+              int ex[3];
+              eri_cart(lc, cc, ex);
+              double s = 0.0;
+              for (int tt = 0; tt <= ex[0]; ++tt) {
+                const double e1 = Ec[ex[0]][tt];
+                if (e1 == 0.0) continue;
+                for (int uu = 0; uu <= ex[1]; ++uu) {
+                  const double e2 = Ec[ex[1]][uu];
+                  if (e2 == 0.0) continue;
+                  for (int vv = 0; vv <= ex[2]; ++vv) {
+                    const double e3 = Ec[ex[2]][vv];
+                    if (e3 == 0.0) continue;
+                    const double sg = ((tt + uu + vv) & 1) ? -1.0 : 1.0;
+                    s += sg * e1 * e2 * e3 * Rc[eri_idx(t + tt, u + uu, v + vv)];
+                  }
+                }
+              }
+              s *= pref;
+              double* w = h ? w1 : w0;
+              for (int mc = 0; mc < nsc; ++mc) w[mc] += sc[mc * ncc + cc] * s;
+            }
+          }
+          __syncwarp();  // R buffers are rewritten by the next primitive
+        }
+        // publish W of this primitive pair, then acc[cab] += sum_bra E W
+        for (int h = 0; h < 2; ++h) {
+          const int e = lane + 32 * h;
+          if (e < nW)
+            for (int mc = 0; mc < nsc; ++mc) W[e * kEriMaxSph + mc] = h ? w1[mc] : w0[mc];
+        }
+        __syncwarp();
+        const double* E = o + 6;
+        for (int h = 0; h < 2; ++h) {
+          const int cab = lane + 32 * h;
+          if (cab >= nca * ncb) break;
+          int ea[3], eb[3];
+          eri_cart(la, cab / ncb, ea);
+          eri_cart(lb, cab % ncb, eb);
+          for (int t = 0; t <= ea[0] + eb[0]; ++t) {
+            const double ex = E[0 * Eax + ea[0] * Esi + eb[0] * Esj + t];
+            if (ex == 0.0) continue;
+            for (int u = 0; u <= ea[1] + eb[1]; ++u) {
+              const double ey = E[1 * Eax + ea[1] * Esi + eb[1] * Esj + u];
+              if (ey == 0.0) continue;
+              for (int v = 0; v <= ea[2] + eb[2]; ++v) {
+                const double ez = E[2 * Eax + ea[2] * Esi + eb[2] * Esj + v];
+                if (ez == 0.0) continue;
+                const double cf = ex * ey * ez;
+                const double* w = W + eri_idx(t, u, v) * kEriMaxSph;
+                double* ac = h ? acc1 : acc0;
+                for (int mc = 0; mc < nsc; ++mc) ac[mc] += cf * w[mc];
+              }
+            }
+          }
+        }
+        __syncwarp();
+      }
+      // spherical (a, b): stage the cartesian accumulators in the warp's
+      // R/W space, then each lane writes outputs (ma, mb, mc)
+      double* st = wbase;
+      for (int h = 0; h < 2; ++h) {
+        const int cab = lane + 32 * h;
+        if (cab < nca * ncb)
+          for (int mc = 0; mc < nsc; ++mc) st[cab * kEriMaxSph + mc] = h ? acc1[mc] : acc0[mc];
+      }
+      __syncwarp();
+      const double* sa = c_eri_sph + eri_sph_off(la);
+      const double* sb = c_eri_sph + eri_sph_off(lb);
+      const int I0 = blk_bf_off[I], J0 = blk_bf_off[J];
+      const int KI = panel_K[I], KJ = panel_K[J];
+      double* PI = B + panel_off[I];
+      double* PJ = B + panel_off[J];
+      for (int o = lane; o < nsa * nsb * nsc; o += 32) {
+        const int ma = o / (nsb * nsc), mb = (o / nsc) % nsb, mc = o % nsc;
+        double v = 0.0;
+        for (int ca = 0; ca < nca; ++ca) {
+          const double fa = sa[ma * nca + ca];
+          if (fa == 0.0) continue;
+          double s2 = 0.0;
+          for (int cb = 0; cb < ncb; ++cb)
+            s2 += sb[mb * ncb + cb] * st[(ca * ncb + cb) * kEriMaxSph + mc];
+          v += fa * s2;
+        }
+        const int mu = a.bf_off + ma - I0, nu = b.bf_off + mb - J0;
+        const long long X = c.bf_off + mc;
+        PI[((long long)mu * naux + X) * KI + col_IJ[it.p] + nu] = v;
+        if (I != J)
+          PJ[((long long)nu * naux + X) * KJ + col_JI[it.p] + mu] = v;
+        else if (it.a != it.b)
+          PI[((long long)nu * naux + X) * KI + col_IJ[it.p] + mu] = v;
+      }
+      __syncwarp();
+    }
+  }
+}
+
+}  // namespace gbjk

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "gbjk.h"
 #include "aok_host.cuh"
+#include "eri3c_gpu.cuh"
 #include "asymk_host.cuh"
 #include "kernels_fp64.cuh"
 #include "mp2_host.cuh"
@@ -704,6 +705,115 @@ gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, doub
     CKL(PH_GATHER);
   }
   CK(cudaStreamSynchronize(ctx->stream));
+  ctx->have_B = true;
+  ctx->ws_nocc = -1;
+  ctx->mp2.release();
+  ctx->aok.release();
+  ctx->asymk.release();
+  ctx->split.invalidate_b();
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk_shells* aux,
+                                const double* sph, const int* blk_shell_off, int nablk,
+                                const int* ablk_shell_off, int npairs, const int* pair_I,
+                                const int* pair_J, const unsigned char* keep, const int* col_IJ,
+                                const int* col_JI) {
+  if (!ctx || !ao || !aux || !sph || !blk_shell_off || !ablk_shell_off || !pair_I || !pair_J ||
+      !keep || !col_IJ || !col_JI || npairs <= 0 || nablk <= 0)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_eri3c: null argument");
+  for (int s = 0; s < ao->nshell; ++s)
+    if (ao->l[s] < 0 || ao->l[s] > kEriMaxLao)
+      return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_eri3c: AO shells above d are not supported");
+  for (int s = 0; s < aux->nshell; ++s)
+    if (aux->l[s] < 0 || aux->l[s] > kEriMaxLaux)
+      return fail(ctx, GBJK_INVALID_ARG,
+                  "gbjk_upload_b_eri3c: auxiliary shells above f are not supported");
+  CK(cudaSetDevice(ctx->device));
+  // host-side tables: shells, primitives, work items (AO shell pairs)
+  auto shells = [](const gbjk_shells* b, std::vector<EriShell>& out) {
+    out.resize(b->nshell);
+    int p0 = 0;
+    for (int s = 0; s < b->nshell; ++s) {
+      out[s].l = b->l[s];
+      out[s].nprim = b->nprim[s];
+      out[s].prim0 = p0;
+      out[s].bf_off = b->bf_off[s];
+      for (int d = 0; d < 3; ++d) out[s].A[d] = b->centers[3 * s + d];
+      p0 += b->nprim[s];
+    }
+    return p0;
+  };
+  std::vector<EriShell> hao, hax;
+  const int npa = shells(ao, hao), npx = shells(aux, hax);
+  std::vector<EriItem> items;
+  size_t bra_max = 0;
+  for (int p = 0; p < npairs; ++p) {
+    const int I = pair_I[p], J = pair_J[p];
+    if (I < 0 || J < I || J >= ctx->nblk)
+      return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_eri3c: bad block pair");
+    for (int a = blk_shell_off[I]; a < blk_shell_off[I + 1]; ++a)
+      for (int b = blk_shell_off[J]; b < blk_shell_off[J + 1]; ++b) {
+        if (I == J && b < a) continue;
+        items.push_back({p, a, b});
+        const int la = hao[a].l, lb = hao[b].l;
+        const size_t psz = 6 + 3 * (la + 1) * (lb + 1) * (la + lb + 1);
+        bra_max = std::max(bra_max, (size_t)hao[a].nprim * hao[b].nprim * psz);
+      }
+  }
+  const size_t smem = (bra_max + (size_t)kEriWarps * kEriWarpDoubles) * sizeof(double);
+  if (smem > 200 * 1024)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_eri3c: contraction too long for the kernel");
+  gbjk_status s;
+  if ((s = dalloc(ctx, &ctx->d_B, (size_t)ctx->nnz))) return s;
+  CK(cudaMemsetAsync(ctx->d_B, 0, (size_t)ctx->nnz * sizeof(double), ctx->stream));
+  // device copies (temporary)
+  std::vector<void*> tmp;
+  auto up = [&](const void* src, size_t bytes, void** dst) -> cudaError_t {
+    cudaError_t e = cudaMalloc(dst, std::max<size_t>(bytes, 1));
+    if (e != cudaSuccess) return e;
+    tmp.push_back(*dst);
+    return cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice);
+  };
+  void *d_items, *d_ao, *d_ax, *d_aoa, *d_aoc, *d_axa, *d_axc, *d_pI, *d_pJ, *d_keep, *d_aoff,
+      *d_cij, *d_cji;
+  cudaError_t e = cudaSuccess;
+  if (!e) e = up(items.data(), items.size() * sizeof(EriItem), &d_items);
+  if (!e) e = up(hao.data(), hao.size() * sizeof(EriShell), &d_ao);
+  if (!e) e = up(hax.data(), hax.size() * sizeof(EriShell), &d_ax);
+  if (!e) e = up(ao->alpha, (size_t)npa * 8, &d_aoa);
+  if (!e) e = up(ao->coef, (size_t)npa * 8, &d_aoc);
+  if (!e) e = up(aux->alpha, (size_t)npx * 8, &d_axa);
+  if (!e) e = up(aux->coef, (size_t)npx * 8, &d_axc);
+  if (!e) e = up(pair_I, (size_t)npairs * 4, &d_pI);
+  if (!e) e = up(pair_J, (size_t)npairs * 4, &d_pJ);
+  if (!e) e = up(keep, (size_t)npairs * nablk, &d_keep);
+  if (!e) e = up(ablk_shell_off, (size_t)(nablk + 1) * 4, &d_aoff);
+  if (!e) e = up(col_IJ, (size_t)npairs * 4, &d_cij);
+  if (!e) e = up(col_JI, (size_t)npairs * 4, &d_cji);
+  if (!e) e = cudaMemcpyToSymbol(c_eri_sph, sph, sizeof(double) * (1 + 9 + 30 + 70));
+  if (!e) e = cudaFuncSetAttribute(k_eri3c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (!e && !items.empty()) {
+    {
+      PhaseScope ps(ctx, PH_GATHER);
+      for (size_t i0 = 0; i0 < items.size(); i0 += (1u << 30)) {
+        const int n = (int)std::min<size_t>(1u << 30, items.size() - i0);
+        k_eri3c<<<n, 32 * kEriWarps, smem, ctx->stream>>>(
+            (const EriItem*)d_items + i0, (const EriShell*)d_ao, (const EriShell*)d_ax,
+            (const double*)d_aoa, (const double*)d_aoc, (const double*)d_axa,
+            (const double*)d_axc, (const int*)d_pI, (const int*)d_pJ,
+            (const unsigned char*)d_keep, nablk, (const int*)d_aoff, ctx->d_boff,
+            ctx->d_panel_off, ctx->d_panelK, (const int*)d_cij, (const int*)d_cji, ctx->naux,
+            ctx->d_B);
+        ctx->launches++;
+      }
+    }
+    e = cudaGetLastError();
+    if (!e) e = cudaStreamSynchronize(ctx->stream);
+  }
+  for (void* p : tmp) cudaFree(p);
+  if (e != cudaSuccess)
+    return fail(ctx, GBJK_CUDA_ERROR, std::string("gbjk_upload_b_eri3c: ") + cudaGetErrorString(e));
   ctx->have_B = true;
   ctx->ws_nocc = -1;
   ctx->mp2.release();

@@ -416,6 +416,38 @@ int gbints_basis_create(gbints_basis** out, int nshell, const int* l, const int*
 
 void gbints_basis_destroy(gbints_basis* b) { delete b; }
 
+// Normalised shell data as the engine uses it (contraction coefficients
+// after gto_normalize); arrays sized by the caller: nshell entries of l,
+// nprim and bf_off, 3 * nshell centres, sum(nprim) exponents and
+// coefficients.
+int gbints_basis_shells(const gbints_basis* b, int* l, int* nprim, int* bf_off, double* centers,
+                        double* alpha, double* coef) {
+  if (!b) return 1;
+  int poff = 0;
+  for (size_t s = 0; s < b->b.shells.size(); ++s) {
+    const Shell& sh = b->b.shells[s];
+    l[s] = sh.l;
+    nprim[s] = (int)sh.alpha.size();
+    bf_off[s] = sh.bf_off;
+    for (int d = 0; d < 3; ++d) centers[3 * s + d] = sh.A[d];
+    for (size_t i = 0; i < sh.alpha.size(); ++i) {
+      alpha[poff + i] = sh.alpha[i];
+      coef[poff + i] = sh.coef[i];
+    }
+    poff += (int)sh.alpha.size();
+  }
+  return 0;
+}
+
+// Cartesian -> real-spherical table of shell l: (2l+1) x (l+1)(l+2)/2,
+// row-major, output order as the integral routines (p: x, y, z).
+int gbints_sph_coeffs(int l, double* out) {
+  if (l < 0 || l > kMaxL || !out) return 1;
+  const auto& t = sph_coeffs(l);
+  std::copy(t.begin(), t.end(), out);
+  return 0;
+}
+
 int gbints_basis_nbf(const gbints_basis* b) { return b ? b->b.nbf : -1; }
 
 int gbints_one_electron(const gbints_basis* bs, int which, int natom, const double* Z,

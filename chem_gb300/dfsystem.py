@@ -55,14 +55,18 @@ def metric_factors(V):
     return Linv, Vinv
 
 
-def build_dfsystem(mol: Molecule, eps=1e-10, one_electron=True, nthreads=0) -> DFSystem:
+def build_dfsystem(mol: Molecule, eps=1e-10, one_electron=True, nthreads=0,
+                   device_ints=False) -> DFSystem:
+    """device_ints: leave the 3-center tensor to the device engine
+    (B = ("device_ints", mol), computed by gbjk_upload_b_eri3c when the J/K
+    engine is created) instead of computing it on the host."""
     t = {}
     t0 = time.perf_counter()
     Zmn, zx = ints.schwarz(mol, nthreads)
     layout = schwarz_layout(mol, Zmn, zx, eps)
     t["schwarz"] = time.perf_counter() - t0
     t0 = time.perf_counter()
-    B = ints.eri3c_panels(mol, layout, nthreads)
+    B = ("device_ints", mol) if device_ints else ints.eri3c_panels(mol, layout, nthreads)
     t["eri3c"] = time.perf_counter() - t0
     t0 = time.perf_counter()
     V = ints.coulomb_metric(mol, nthreads)

@@ -29,6 +29,12 @@ STATUS = {0: "OK", 1: "INVALID_ARG", 2: "OOM", 3: "CUDA_ERROR", 4: "TIMEOUT",
           5: "NOT_CONVERGED", 6: "NOT_READY"}
 
 
+class GbjkShells(C.Structure):
+    _fields_ = [("nshell", C.c_int), ("l", C.POINTER(C.c_int)), ("nprim", C.POINTER(C.c_int)),
+                ("bf_off", C.POINTER(C.c_int)), ("centers", C.POINTER(C.c_double)),
+                ("alpha", C.POINTER(C.c_double)), ("coef", C.POINTER(C.c_double))]
+
+
 class GbjkDesc(C.Structure):
     _fields_ = [("nbf", C.c_int), ("naux", C.c_int), ("nblk", C.c_int),
                 ("blk_size", C.POINTER(C.c_int)), ("panel_K", C.POINTER(C.c_int)),
@@ -61,6 +67,10 @@ def lib():
         L.gbjk_set_aux_batch.argtypes = [vp, C.c_int]
         L.gbjk_upload_b_synthetic.argtypes = [vp, C.c_ulonglong, C.c_double]
         L.gbjk_download_b.argtypes = [vp, dp]
+        ip = C.POINTER(C.c_int)
+        L.gbjk_upload_b_eri3c.argtypes = [vp, C.POINTER(GbjkShells), C.POINTER(GbjkShells), dp,
+                                          ip, C.c_int, ip, C.c_int, ip, ip,
+                                          C.POINTER(C.c_ubyte), ip, ip]
         L.gbjk_compute_j.argtypes = [vp, dp, dp]
         L.gbjk_compute_k.argtypes = [vp, C.c_int, dp, C.c_int, dp]
         L.gbjk_compute_jk.argtypes = [vp, C.c_int, dp, dp, C.c_int, dp, dp]
@@ -135,7 +145,9 @@ class JKEngine:
             self._check(L.gbjk_set_fitted(h, 1), "gbjk_set_fitted")
         if aux_batch:
             self._check(L.gbjk_set_aux_batch(h, int(aux_batch)), "gbjk_set_aux_batch")
-        if B is None:
+        if isinstance(B, tuple) and B and B[0] == "device_ints":
+            self.upload_b_device_ints(B[1])
+        elif B is None:
             if synthetic is None:
                 raise ValueError("B or synthetic=(seed, decay) is required")
             seed, decay = synthetic
@@ -188,6 +200,33 @@ class JKEngine:
             _dp(J) if J is not None else None, _dp(K) if K is not None else None),
             "gbjk_compute_jk")
         return J, K
+
+    def upload_b_device_ints(self, mol):
+        """Compute the 3-center tensor on the device (gbjk_upload_b_eri3c)
+        for molecule `mol` on this engine's layout."""
+        from . import ints
+        lay = self.layout
+        keep_alive = []
+
+        def shells(basis):
+            d = ints.shell_arrays(basis)
+            keep_alive.append(d)
+            ptr = lambda a, t: a.ctypes.data_as(C.POINTER(t))
+            return GbjkShells(len(d["l"]), ptr(d["l"], C.c_int), ptr(d["nprim"], C.c_int),
+                              ptr(d["bf_off"], C.c_int), ptr(d["centers"], C.c_double),
+                              ptr(d["alpha"], C.c_double), ptr(d["coef"], C.c_double))
+        ao, ax = shells(mol.basis), shells(mol.dfbasis)
+        sph = ints.sph_tables(3)
+        arr = {k: np.ascontiguousarray(v, np.int32) for k, v in (
+            ("boff", mol.basis.block_shell_off), ("aoff", mol.dfbasis.block_shell_off),
+            ("pI", lay.pair_I), ("pJ", lay.pair_J), ("cij", lay.col_IJ), ("cji", lay.col_JI))}
+        keep = np.ascontiguousarray(lay.keep, np.uint8)
+        ip = lambda a: a.ctypes.data_as(C.POINTER(C.c_int))
+        self._check(lib().gbjk_upload_b_eri3c(
+            self.h, C.byref(ao), C.byref(ax), _dp(sph), ip(arr["boff"]), lay.nablk,
+            ip(arr["aoff"]), len(arr["pI"]), ip(arr["pI"]), ip(arr["pJ"]),
+            keep.ctypes.data_as(C.POINTER(C.c_ubyte)), ip(arr["cij"]), ip(arr["cji"])),
+            "gbjk_upload_b_eri3c")
 
     def compute_k_ao(self, P):
         """DF-AO K (gbjk_compute_k_ao) from the alpha density P; K negated."""

@@ -36,6 +36,8 @@ def lib():
         L.gbints_eri4c.argtypes = [C.c_void_p, _dp, C.c_int]
         L.gbints_schwarz_pairs.argtypes = [C.c_void_p, _dp, C.c_int]
         L.gbints_schwarz_aux.argtypes = [C.c_void_p, _dp, C.c_int]
+        L.gbints_basis_shells.argtypes = [C.c_void_p, _ip, _ip, _ip, _dp, _dp, _dp]
+        L.gbints_sph_coeffs.argtypes = [C.c_int, _dp]
         L.gbints_eri3c_panels.argtypes = [
             C.c_void_p, C.c_void_p, C.c_int, _ip, C.c_int, _ip, C.c_int, _ip, _ip,
             C.POINTER(C.c_ubyte), C.POINTER(C.c_longlong), _ip, _ip, _ip, _dp, C.c_int]
@@ -132,3 +134,28 @@ def eri3c_panels(mol: Molecule, layout, nthreads=0):
         _p(pI, _ip), _p(pJ, _ip), _p(keep, C.POINTER(C.c_ubyte)), _p(poff, C.POINTER(C.c_longlong)),
         _p(pK, _ip), _p(cij, _ip), _p(cji, _ip), _p(B), nthreads), "gbints_eri3c_panels")
     return B
+
+
+def shell_arrays(basis: Basis):
+    """Normalised shell data of a basis as the host engine uses it (for the
+    device integral engine): dict of l, nprim, bf_off, centers, alpha, coef."""
+    bh = BasisHandle(basis)
+    n = bh.nshell
+    npr = sum(len(s.alpha) for s in basis.shells)
+    out = {"l": np.zeros(n, np.int32), "nprim": np.zeros(n, np.int32),
+           "bf_off": np.zeros(n, np.int32), "centers": np.zeros(3 * n),
+           "alpha": np.zeros(npr), "coef": np.zeros(npr)}
+    _check(lib().gbints_basis_shells(bh.h, _p(out["l"], _ip), _p(out["nprim"], _ip),
+                                     _p(out["bf_off"], _ip), _p(out["centers"]),
+                                     _p(out["alpha"]), _p(out["coef"])), "gbints_basis_shells")
+    return out
+
+
+def sph_tables(lmax=3):
+    """Concatenated cartesian -> spherical tables for l = 0..lmax."""
+    parts = []
+    for l in range(lmax + 1):
+        t = np.zeros((2 * l + 1) * (l + 1) * (l + 2) // 2)
+        _check(lib().gbints_sph_coeffs(l, _p(t)), "gbints_sph_coeffs")
+        parts.append(t)
+    return np.concatenate(parts)

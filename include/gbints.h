@@ -33,6 +33,12 @@ int gbints_basis_create(gbints_basis** out, int nshell, const int* l, const int*
                         const double* centers, const double* alpha, const double* coef);
 void gbints_basis_destroy(gbints_basis* b);
 int gbints_basis_nbf(const gbints_basis* b);
+/* Normalised shell data (coefficients after gto_normalize) for a device
+ * integral engine; no counterpart in the reference. */
+int gbints_basis_shells(const gbints_basis* b, int* l, int* nprim, int* bf_off, double* centers,
+                        double* alpha, double* coef);
+/* Cartesian -> real-spherical table of shell l, (2l+1) x (l+1)(l+2)/2. */
+int gbints_sph_coeffs(int l, double* out);
 
 /* which: 0 overlap, 1 kinetic, 2 nuclear attraction (charges Z[natom], xyz
  * [natom*3] in bohr).  M is nbf x nbf row-major. */

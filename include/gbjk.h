@@ -109,6 +109,32 @@ gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows);
 gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, double decay);
 gbjk_status gbjk_download_b(gbjk_ctx* ctx, double* B);
 
+/* Shells of a basis, normalised as the host engine uses them (the output of
+ * gbints_basis_shells): per shell l, primitive count, first basis function,
+ * centre (3 doubles); exponents and contraction coefficients concatenated. */
+typedef struct gbjk_shells {
+  int nshell;
+  const int* l;
+  const int* nprim;
+  const int* bf_off;
+  const double* centers;
+  const double* alpha;
+  const double* coef;
+} gbjk_shells;
+/* Compute the 3-center tensor on the device straight into the panel layout
+ * (replaces the host calc_ints 3c2e pass, src/ints/integrals.cpp:250-370,
+ * and gbjk_upload_b): AO block pairs pair_I[p] <= pair_J[p] with their
+ * panel columns col_IJ / col_JI, keep[p * nablk + A] the kept auxiliary
+ * blocks, blk_shell_off / ablk_shell_off the shell ranges of the AO and
+ * auxiliary blocks, sph the cartesian -> spherical tables of l = 0..3
+ * (gbints_sph_coeffs, concatenated).  AO shells up to d, auxiliary shells up
+ * to f.  No counterpart in the reference (its integrals run on the host). */
+gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk_shells* aux,
+                                const double* sph, const int* blk_shell_off, int nablk,
+                                const int* ablk_shell_off, int npairs, const int* pair_I,
+                                const int* pair_J, const unsigned char* keep, const int* col_IJ,
+                                const int* col_JI);
+
 /* jmode: GBJK_J_VINV (default, the reference route) or GBJK_J_CHOLESKY.
  * No counterpart in the reference. */
 gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode);
