@@ -268,11 +268,13 @@ struct AsymKState {
       w.ncol1 = 1 << 30;
       return w;
     };
+    // both sides' tiles of one A row tile are adjacent: its digits come
+    // from HBM once and from L2 for the other side
     i_ht0 = 0;
-    for (int side = 0; side < 2; ++side)
-      for (int I = 0; I < nblk; ++I) {
-        const long long rows = (long long)(*L.bsize)[I] * naux;
-        for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
+    for (int I = 0; I < nblk; ++I) {
+      const long long rows = (long long)(*L.bsize)[I] * naux;
+      for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
+        for (int side = 0; side < 2; ++side)
           for (int nt = 0; nt < cdiv_(nocc, kTileN); ++nt) {
             SplitItem w = base();
             w.a = sp.d_Aslices + sp.a_off[I];
@@ -296,7 +298,7 @@ struct AsymKState {
             w.emax_div = naux;
             items.push_back(w);
           }
-      }
+    }
     i_htn = (int)items.size() - i_ht0;
     i_k0 = (int)items.size();
     for (int k = 0; k < ksplit; ++k) {

@@ -415,11 +415,14 @@ struct Mp2State {
       w.ncol1 = 1 << 30;
       return w;
     };
+    // T1 items: the points' tiles of one A row tile are adjacent in the list
+    // (and so run at the same time on different SMs), so the L^-1 B digit
+    // tile is read from HBM once for all points and then served from L2
     i1_0 = 0;
-    for (int t = 0; t < npts; ++t)
-      for (int I = 0; I < nblk; ++I) {
-        const long long rows = (long long)bsize[I] * naux;
-        for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
+    for (int I = 0; I < nblk; ++I) {
+      const long long rows = (long long)bsize[I] * naux;
+      for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
+        for (int t = 0; t < npts; ++t)
           for (int nt = 0; nt < cdiv_(ro[t], kTileN); ++nt) {
             SplitItem w = base_item();
             w.a = sp.d_Aslices + sp.a_off[I];
@@ -439,7 +442,7 @@ struct Mp2State {
             w.n_valid = std::min(kTileN, ro[t] - nt * kTileN);
             items.push_back(w);
           }
-      }
+    }
     i1_n = (int)items.size();
     i2_0 = (int)items.size();
     for (int t = 0; t < npts; ++t)
