@@ -139,6 +139,24 @@ class ClockSampler:
                 "samples": len(self.samples)}
 
 
+def max_over_ranks(x, world, device=None):
+    """Replicas: each rank times its own copy of the workload; the job's time
+    is the slowest rank's (all-reduce MAX; NCCL on the GPUs, any backend the
+    process group was started with)."""
+    if world <= 1:
+        return float(x)
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(ms_per_step, world):
+    """Whole-job throughput of `world` replicas (builds/s over all ranks)."""
+    return world * 1e3 / ms_per_step
+
+
 def peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -511,12 +529,8 @@ def main():
         eng.synchronize()
     torch.cuda.synchronize()
     launches = eng.kernel_launches - launches0
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1e3 / ms
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world, dev)
+    value = replica_value(ms, world)
 
     # per-phase device time (CUDA events around every launch), same builds
     # issued directly rather than through the graph
@@ -539,11 +553,7 @@ def main():
         Jh, Kh = eng.compute_jk(Ph, Cocc, args.kmethod)
     e1.record(stream)
     torch.cuda.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, dev)
 
     # roofline of the dominant phase
     hbm, bf16, bf16s, src = peaks()
