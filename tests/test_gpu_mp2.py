@@ -36,9 +36,10 @@ def _engine(ds, precision):
     return JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=ds.eps, precision=precision)
 
 
-def test_mp2_fp64_matches_oracle_bitwise(ethane):
+@pytest.mark.parametrize("sysname", ["ethane", "decane"])
+def test_mp2_fp64_matches_oracle_bitwise(sysname, request):
     from oracle import oracle as O
-    ds, f = ethane
+    ds, f = request.getfixturevalue(sysname)
     eng = _engine(ds, "fp64")
     e, Z = eng.mp2_laplace(f.Lo, f.Lv, want_z=True)
     orc = O.Oracle(ds.layout, ds.B)
