@@ -55,6 +55,22 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// One Fock build recorded as a CUDA graph, valid while the engine epoch it
+// was captured at is current.
+struct CapturedBuild {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int64_t launches = 0;
+  uint64_t epoch = 0;
+  void reset() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    launches = 0;
+  }
+};
+
 struct gbjk_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -112,10 +128,14 @@ struct gbjk_ctx {
   int64_t ph_launch[PH_COUNT] = {};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
   std::vector<cudaEvent_t> ev_pool;
-  // captured Fock build
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t graph_exec = nullptr;
-  int64_t graph_launch_count = 0;
+  // captured Fock builds: the caller's (device pointers) and the host-buffer
+  // call's own (context buffers, keyed by its arguments' shape)
+  CapturedBuild user_graph, host_graph;
+  int host_kmethod = -1, host_nocc = -1;
+  bool host_j = false, host_k = false, host_uncapturable = false;
+  // bumped by every free or replacement of a buffer and by every setting
+  // that changes the launch sequence; a captured build older than it is stale
+  uint64_t epoch = 0;
 };
 
 namespace {
@@ -162,6 +182,7 @@ gbjk_status dalloc(gbjk_ctx* ctx, T** p, size_t count) {
 template <class T>
 void dfree(gbjk_ctx* ctx, T** p) {
   if (*p) {
+    ctx->epoch++;
     cudaFree(*p);
     auto it = ctx->alloc_bytes.find((void*)*p);
     if (it != ctx->alloc_bytes.end()) {
@@ -619,8 +640,8 @@ void gbjk_destroy(gbjk_ctx* ctx) {
     cudaEventDestroy(pe.second.second);
   }
   for (auto e : ctx->ev_pool) cudaEventDestroy(e);
-  if (ctx->graph_exec) cudaGraphExecDestroy(ctx->graph_exec);
-  if (ctx->graph) cudaGraphDestroy(ctx->graph);
+  ctx->user_graph.reset();
+  ctx->host_graph.reset();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -665,6 +686,7 @@ gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices) {
     return fail(ctx, GBJK_INVALID_ARG, "unknown precision");
   if (nslices < 0 || nslices > kMaxSlices)
     return fail(ctx, GBJK_INVALID_ARG, "nslices out of range");
+  ctx->epoch++;
   ctx->precision = precision;
   ctx->nslices = nslices;
   return GBJK_OK;
@@ -672,6 +694,7 @@ gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices) {
 
 gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
   if (!ctx) return GBJK_INVALID_ARG;
+  ctx->epoch++;
   ctx->fitted = fitted != 0;
   ctx->split.fitted = ctx->fitted;
   ctx->mp2.release();
@@ -684,6 +707,7 @@ gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
 
 gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows) {
   if (!ctx || rows < 0) return GBJK_INVALID_ARG;
+  ctx->epoch++;
   ctx->split.xb_req = rows;
   ctx->mp2.release();
   ctx->aok.release();
@@ -834,6 +858,7 @@ gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode) {
   if (!ctx) return GBJK_INVALID_ARG;
   if (jmode != GBJK_J_VINV && jmode != GBJK_J_CHOLESKY)
     return fail(ctx, GBJK_INVALID_ARG, "unknown J mode");
+  ctx->epoch++;
   ctx->jmode = jmode;
   return GBJK_OK;
 }
@@ -926,6 +951,53 @@ gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, co
   return GBJK_OK;
 }
 
+static uint64_t build_epoch(const gbjk_ctx* ctx) { return ctx->epoch + ctx->split.frees; }
+
+// Record one device-pointer Fock build (plans and buffers already prepared
+// by an ordinary build) as a CUDA graph on the context's stream.
+static gbjk_status capture_build(gbjk_ctx* ctx, CapturedBuild& cb, int kmethod, const double* dP,
+                                 const double* dC, int nocc, double* dJ, double* dK) {
+  cb.reset();
+  const uint64_t ep = build_epoch(ctx);
+  const bool prof = ctx->profile;
+  ctx->profile = false;
+  ctx->split.profile = false;
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) {
+    ctx->profile = prof;
+    ctx->split.profile = prof;
+    return fail(ctx, GBJK_CUDA_ERROR, std::string("graph capture: ") + cudaGetErrorString(e));
+  }
+  const int64_t l0 = ctx->launches;
+  gbjk_status s = gbjk_compute_jk_dev(ctx, kmethod, dP, dC, nocc, dJ, dK);
+  const int64_t n = ctx->launches - l0;
+  ctx->launches = l0;
+  cudaGraph_t g = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &g);
+  ctx->profile = prof;
+  ctx->split.profile = prof;
+  if (s || e != cudaSuccess || build_epoch(ctx) != ep) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (s) return s;
+    return fail(ctx, GBJK_CUDA_ERROR,
+                e != cudaSuccess ? std::string("graph capture: ") + cudaGetErrorString(e)
+                                 : std::string("graph capture: the build replaced engine buffers"));
+  }
+  cudaGraphExec_t x = nullptr;
+  e = cudaGraphInstantiate(&x, g, 0);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    return fail(ctx, GBJK_CUDA_ERROR, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  }
+  cb.graph = g;
+  cb.exec = x;
+  cb.launches = n;
+  cb.epoch = ep;
+  return GBJK_OK;
+}
+
 gbjk_status gbjk_capture_graph(gbjk_ctx* ctx, int kmethod, const double* dP, const double* dC,
                                int nocc, double* dJ, double* dK) {
   gbjk_status s;
@@ -934,41 +1006,20 @@ gbjk_status gbjk_capture_graph(gbjk_ctx* ctx, int kmethod, const double* dP, con
   // that the captured sequence contains launches and memsets only
   if ((s = gbjk_compute_jk_dev(ctx, kmethod, dP, dC, nocc, dJ, dK))) return s;
   if ((s = gbjk_synchronize(ctx))) return s;
-  const bool prof = ctx->profile;
-  ctx->profile = false;
-  ctx->split.profile = false;
-  if (ctx->graph_exec) {
-    cudaGraphExecDestroy(ctx->graph_exec);
-    ctx->graph_exec = nullptr;
-  }
-  if (ctx->graph) {
-    cudaGraphDestroy(ctx->graph);
-    ctx->graph = nullptr;
-  }
-  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-  const int64_t l0 = ctx->launches;
-  s = gbjk_compute_jk_dev(ctx, kmethod, dP, dC, nocc, dJ, dK);
-  ctx->graph_launch_count = ctx->launches - l0;
-  ctx->launches = l0;
-  cudaGraph_t g = nullptr;
-  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
-  ctx->profile = prof;
-  ctx->split.profile = prof;
-  if (s) {
-    if (g) cudaGraphDestroy(g);
-    return s;
-  }
-  if (e != cudaSuccess) return fail(ctx, GBJK_CUDA_ERROR, std::string("graph capture: ") + cudaGetErrorString(e));
-  ctx->graph = g;
-  CK(cudaGraphInstantiate(&ctx->graph_exec, g, 0));
-  return GBJK_OK;
+  return capture_build(ctx, ctx->user_graph, kmethod, dP, dC, nocc, dJ, dK);
 }
 
 gbjk_status gbjk_launch_graph(gbjk_ctx* ctx) {
   if (!ctx) return GBJK_INVALID_ARG;
-  if (!ctx->graph_exec) return fail(ctx, GBJK_NOT_READY, "no captured build");
-  CK(cudaGraphLaunch(ctx->graph_exec, ctx->stream));
-  ctx->launches += ctx->graph_launch_count;
+  CapturedBuild& cb = ctx->user_graph;
+  if (!cb.exec) return fail(ctx, GBJK_NOT_READY, "no captured build");
+  if (cb.epoch != build_epoch(ctx)) {
+    cb.reset();
+    return fail(ctx, GBJK_NOT_READY,
+                "engine buffers or settings changed since the build was captured; capture again");
+  }
+  CK(cudaGraphLaunch(cb.exec, ctx->stream));
+  ctx->launches += cb.launches;
   return GBJK_OK;
 }
 
@@ -1003,12 +1054,52 @@ gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* P, const d
     if (!P) return fail(ctx, GBJK_INVALID_ARG, "missing density");
     CK(cudaMemcpyAsync(ctx->d_P, P, n2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
   }
-  if ((s = gbjk_compute_jk_dev(ctx, kmethod, J ? ctx->d_P : nullptr, K ? ctx->d_C : nullptr,
-                               nocc, J ? ctx->d_J : nullptr, K ? ctx->d_K : nullptr)))
+  const int key_nocc = K ? nocc : 0;
+  const bool same_shape = ctx->host_kmethod == kmethod && ctx->host_nocc == key_nocc &&
+                          ctx->host_j == (J != nullptr) && ctx->host_k == (K != nullptr) &&
+                          ctx->host_graph.epoch == build_epoch(ctx);
+  const bool replay = !ctx->profile && same_shape && ctx->host_graph.exec;
+  if (replay) {
+    CK(cudaGraphLaunch(ctx->host_graph.exec, ctx->stream));
+    ctx->launches += ctx->host_graph.launches;
+  } else if ((s = gbjk_compute_jk_dev(ctx, kmethod, J ? ctx->d_P : nullptr, K ? ctx->d_C : nullptr,
+                                      nocc, J ? ctx->d_J : nullptr, K ? ctx->d_K : nullptr))) {
     return s;
+  }
   if (J) CK(cudaMemcpyAsync(J, ctx->d_J, n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   if (K) CK(cudaMemcpyAsync(K, ctx->d_K, n2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-  return gbjk_synchronize(ctx);
+  if ((s = gbjk_synchronize(ctx))) return s;
+  if (!replay && !ctx->profile && !(same_shape && ctx->host_uncapturable)) {
+    // record this shape for the next call; a build that cannot be captured
+    // keeps its direct launches
+    ctx->host_kmethod = kmethod;
+    ctx->host_nocc = key_nocc;
+    ctx->host_j = J != nullptr;
+    ctx->host_k = K != nullptr;
+    const std::string err = ctx->err;
+    ctx->host_uncapturable =
+        capture_build(ctx, ctx->host_graph, kmethod, J ? ctx->d_P : nullptr,
+                      K ? ctx->d_C : nullptr, nocc, J ? ctx->d_J : nullptr,
+                      K ? ctx->d_K : nullptr) != GBJK_OK;
+    if (ctx->host_uncapturable) {
+      ctx->host_graph.epoch = build_epoch(ctx);
+      ctx->err = err;
+    }
+  }
+  return GBJK_OK;
+}
+
+void* gbjk_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes ? bytes : 1, cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+
+void gbjk_host_free(void* p) {
+  if (p) cudaFreeHost(p);
 }
 
 gbjk_status gbjk_compute_j(gbjk_ctx* ctx, const double* P, double* J) {

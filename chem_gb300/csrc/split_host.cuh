@@ -23,6 +23,7 @@ namespace gbjk {
 
 struct SplitState {
   size_t bytes = 0;
+  uint64_t frees = 0;  // buffers freed so far (a captured build using them is stale)
   int nbf = 0, naux = 0, nblk = 0;
   std::vector<int> bsize, boff, panelK, cmoff;
   std::vector<long long> panel_off;
@@ -94,7 +95,10 @@ struct SplitState {
   }
   template <class T>
   void free_(T** p) {
-    if (*p) cudaFree(*p);
+    if (*p) {
+      cudaFree(*p);
+      frees++;
+    }
     *p = nullptr;
   }
   void release_build() {

@@ -83,6 +83,9 @@ def lib():
         L.gbjk_capture_graph.argtypes = [vp, C.c_int, C.c_void_p, C.c_void_p, C.c_int,
                                          C.c_void_p, C.c_void_p]
         L.gbjk_launch_graph.argtypes = [vp]
+        L.gbjk_host_alloc.argtypes = [C.c_size_t]
+        L.gbjk_host_alloc.restype = C.c_void_p
+        L.gbjk_host_free.argtypes = [C.c_void_p]
         L.gbjk_stream.argtypes = [vp]
         L.gbjk_stream.restype = C.c_void_p
         L.gbjk_device_bytes.argtypes = [vp]
@@ -115,6 +118,32 @@ def k_split_plan(nbf, naux, nocc):
     if lib().gbjk_k_split_plan(nbf, naux, nocc, C.byref(ks), C.byref(kc)) != 0:
         raise RuntimeError("gbjk_k_split_plan: invalid arguments")
     return ks.value, kc.value
+
+
+class _PinnedBuffer:
+    """Page-locked host bytes from gbjk_host_alloc, freed with the last array
+    that views them."""
+
+    def __init__(self, nbytes):
+        self.ptr = lib().gbjk_host_alloc(max(1, nbytes))
+        if not self.ptr:
+            raise MemoryError(f"gbjk_host_alloc of {nbytes} bytes failed")
+        self.__array_interface__ = {"shape": (nbytes,), "typestr": "|u1",
+                                    "data": (self.ptr, False), "version": 3}
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().gbjk_host_free(self.ptr)
+            self.ptr = None
+
+
+def host_array(shape, dtype=np.float64):
+    """A numpy array in page-locked host memory (gbjk_host_alloc): inputs and
+    outputs of the host-buffer calls in this memory are copied by DMA."""
+    dt = np.dtype(dtype)
+    shape = (shape,) if np.isscalar(shape) else tuple(int(d) for d in shape)
+    nbytes = int(np.prod(shape, dtype=np.int64)) * dt.itemsize
+    return np.asarray(_PinnedBuffer(nbytes))[:nbytes].view(dt).reshape(shape)
 
 
 class JKEngine:
@@ -187,10 +216,23 @@ class JKEngine:
         code = {"vinv": 0, "cholesky": 1}[jmode]
         self._check(lib().gbjk_set_jmode(self.h, code), "gbjk_set_jmode")
 
-    def compute_jk(self, Ptot=None, Cocc=None, kmethod="dfmo"):
+    def compute_jk(self, Ptot=None, Cocc=None, kmethod="dfmo", out=None):
+        """J from the total density and K from the occupied coefficients
+        (gbjk_compute_jk).  `out=(J, K)` writes into caller-owned
+        C-contiguous float64 nbf x nbf arrays, e.g. from host_array(), whose
+        page-locked memory the copies reach by DMA."""
         n = self.nbf
-        J = np.zeros((n, n)) if Ptot is not None else None
-        K = np.zeros((n, n)) if Cocc is not None else None
+        if out is not None:
+            J, K = out
+            for a, want in ((J, Ptot is not None), (K, Cocc is not None)):
+                if want and (a is None or a.shape != (n, n) or a.dtype != np.float64
+                             or not a.flags.c_contiguous or not a.flags.writeable):
+                    raise ValueError("out arrays must be writable C-contiguous float64 nbf x nbf")
+            J = J if Ptot is not None else None
+            K = K if Cocc is not None else None
+        else:
+            J = np.empty((n, n)) if Ptot is not None else None
+            K = np.empty((n, n)) if Cocc is not None else None
         P = np.ascontiguousarray(Ptot, float) if Ptot is not None else None
         Cm = np.ascontiguousarray(Cocc, float) if Cocc is not None else None
         nocc = Cm.shape[1] if Cm is not None else 0

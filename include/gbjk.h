@@ -162,9 +162,19 @@ gbjk_status gbjk_compute_k_ao_dev(gbjk_ctx* ctx, const double* dP, double* dK);
  * The split path uses the Cholesky route of the metric. */
 gbjk_status gbjk_compute_k_lmo_asym(gbjk_ctx* ctx, const double* U, const double* Vt, int nocc,
                                     double* K);
-/* One Fock build: J from Ptot and K from Cocc in one call. */
+/* One Fock build: J from Ptot and K from Cocc in one call.  The first call
+ * for a given (kmethod, nocc, J and/or K) runs the launches directly and
+ * captures them as a CUDA graph on the context's own device buffers; later
+ * calls with the same shape copy the inputs in, replay that graph and copy
+ * J and K out.  Host buffers from gbjk_host_alloc (pinned) are copied by DMA
+ * without staging; any other host memory works too. */
 gbjk_status gbjk_compute_jk(gbjk_ctx* ctx, int kmethod, const double* Ptot, const double* Cocc,
                             int nocc, double* J, double* K);
+/* Page-locked host memory for the inputs and outputs of the host-buffer
+ * calls (cudaHostAlloc, portable).  NULL on failure.  No counterpart in the
+ * reference, whose matrices live in host memory owned by DBCSR. */
+void* gbjk_host_alloc(size_t bytes);
+void gbjk_host_free(void* p);
 
 /* Device-pointer variants, ordered on the context's stream (no host sync). */
 gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dPtot,
@@ -173,7 +183,11 @@ gbjk_status gbjk_synchronize(gbjk_ctx* ctx);
 /* Capture one device-pointer Fock build (same arguments as
  * gbjk_compute_jk_dev) as a CUDA graph on the context's stream, after one
  * ordinary build that prepares every plan; gbjk_launch_graph replays it
- * (same pointers, new contents).  No counterpart in the reference. */
+ * (same pointers, new contents).  A call that frees or replaces any engine
+ * buffer (an upload, gbjk_set_fitted, gbjk_set_aux_batch, a build with
+ * another nocc or precision) discards the captured build, and
+ * gbjk_launch_graph then returns GBJK_NOT_READY.  No counterpart in the
+ * reference. */
 gbjk_status gbjk_capture_graph(gbjk_ctx* ctx, int kmethod, const double* dPtot,
                                const double* dCocc, int nocc, double* dJ, double* dK);
 gbjk_status gbjk_launch_graph(gbjk_ctx* ctx);
