@@ -42,6 +42,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scf", action="store_true")
     ap.add_argument("--no-dfao", action="store_true")
+    ap.add_argument("--no-water", action="store_true")
     ap.add_argument("--workload", default="fock", choices=["fock", "serving", "synthetic", "mp2"])
     ap.add_argument("--mp2-alkane", type=int, default=40)
     ap.add_argument("--mp2-points", type=int, default=8)
@@ -67,11 +68,7 @@ def setup(nC):
     t0 = time.perf_counter()
     ds = build_dfsystem(mol, eps=1e-10)
     tset = time.perf_counter() - t0
-    # core-guess orbitals: diagonalise H in the Loewdin basis
-    sv, U = np.linalg.eigh(ds.S)
-    X = U @ np.diag(sv ** -0.5) @ U.T
-    e, Cp = np.linalg.eigh(X.T @ ds.Hcore @ X)
-    Cocc = np.ascontiguousarray((X @ Cp)[:, :mol.nocc])
+    Cocc = core_guess(ds, mol.nocc)
     P = Cocc @ Cocc.T
     return mol, ds, Cocc, P, tset
 
@@ -164,6 +161,79 @@ def peaks():
             d = json.load(f)
         return d["hbm_gbs"], d["bf16_tflops"], d.get("bf16_tflops_sustained"), "measured"
     return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def core_guess(ds, nocc):
+    """Core-guess orbitals: H diagonalised in the Loewdin basis."""
+    sv, U = np.linalg.eigh(ds.S)
+    X = U @ np.diag(sv ** -0.5) @ U.T
+    _, Cp = np.linalg.eigh(X.T @ ds.Hcore @ X)
+    return np.ascontiguousarray((X @ Cp)[:, :nocc])
+
+
+def run_water(dev, reps=2000):
+    """Water DF-HF Fock build (cc-pVDZ / cc-pVDZ-jkfit; nbf 24, naux 116,
+    nocc 5): launch-bound, so the latency of one build replayed as a CUDA
+    graph is the figure, beside the host-buffer call, the CPU oracle and the
+    FP64 path's agreement with the oracle."""
+    import torch
+    from chem_gb300 import geometry
+    from chem_gb300.dfsystem import build_dfsystem
+    from chem_gb300.fock import JKEngine, host_array
+    from chem_gb300.molecule import molecule_from_angstrom
+    from oracle.oracle import Oracle
+    s, x = geometry.water()
+    mol = molecule_from_angstrom(s, x, "cc-pvdz", "cc-pvdz-jkfit")
+    ds = build_dfsystem(mol, eps=1e-10)
+    C = core_guess(ds, mol.nocc)
+    Pt = 2.0 * C @ C.T
+    n = ds.nbf
+    O = Oracle(ds.layout, ds.B)
+    t0 = time.perf_counter()
+    for _ in range(20):
+        Jo = O.df_j(ds.Vinv, Pt, ds.eps)
+        Ko = O.dfmo_k(np.tril(ds.Linv), C, ds.eps)
+    cpu_us = (time.perf_counter() - t0) / 20 * 1e6
+    res = {"workload": "H2O DF-HF Fock build, cc-pVDZ/cc-pVDZ-jkfit, atom blocks, Schwarz 1e-10",
+           "nbf": n, "naux": ds.naux, "nocc": mol.nocc, "cpu_oracle_us": cpu_us,
+           "cpu_oracle_threads": os.cpu_count()}
+    for prec in ("fp64", "split"):
+        eng = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=ds.eps, precision=prec)
+        st = torch.cuda.ExternalStream(eng.stream, device=dev)
+        dP = torch.from_numpy(Pt).to(dev)
+        dC = torch.from_numpy(C).to(dev)
+        dJ = torch.empty((n, n), dtype=torch.float64, device=dev)
+        dK = torch.empty((n, n), dtype=torch.float64, device=dev)
+        torch.cuda.synchronize()
+        eng.capture_graph(dP.data_ptr(), dC.data_ptr(), mol.nocc, dJ.data_ptr(), dK.data_ptr())
+        for _ in range(20):
+            eng.launch_graph()
+        eng.synchronize()
+        l0 = eng.kernel_launches
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            eng.launch_graph()
+        e1.record(st)
+        eng.synchronize()
+        res[f"{prec}_graph_us"] = e0.elapsed_time(e1) / reps * 1e3
+        res[f"{prec}_launches_per_build"] = (eng.kernel_launches - l0) // reps
+        Ph, Ch = host_array((n, n)), host_array(C.shape)
+        Ph[...], Ch[...] = Pt, C
+        out = (host_array((n, n)), host_array((n, n)))
+        for _ in range(20):
+            eng.compute_jk(Ph, Ch, out=out)
+        t0 = time.perf_counter()
+        for _ in range(reps // 4):
+            eng.compute_jk(Ph, Ch, out=out)
+        res[f"{prec}_e2e_us"] = (time.perf_counter() - t0) / (reps // 4) * 1e6
+        if prec == "fp64":
+            res["fp64_max_abs_dJ_vs_oracle"] = float(np.abs(out[0] - Jo).max())
+            res["fp64_max_abs_dK_vs_oracle"] = float(np.abs(out[1] - Ko).max())
+        else:
+            res["split_max_abs_dK_vs_oracle"] = float(np.abs(out[1] - Ko).max())
+        eng.close()
+    return res
 
 
 def cpu_reference_build(ds, Cocc, P, kchunk):
@@ -738,6 +808,8 @@ def main():
         "clocks": clk.summary(),
         "setup_s": {"integrals_host": round(tset, 2)},
     }
+    if rank == 0 and not args.no_water:
+        out["water"] = run_water(dev)
     if rank == 0 and not args.no_cpu_baseline:
         kc = k_split_plan(nbf, naux, nocc)[1]
         tcpu = cpu_reference_build(ds, Cocc, P, kc)

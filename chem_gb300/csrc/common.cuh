@@ -23,8 +23,8 @@ struct GemmGroup {
 };
 enum : int { kTransB = 1, kLowerA = 2, kAccum = 4 };
 
-// One 64 x 64 output tile of a group, over the k range [k0, k1); the tile is
-// written at C + coff (split-K partial buffers).
+// One output tile of a group (64 rows x 64 or 16 columns), over the k range
+// [k0, k1); the tile is written at C + coff (split-K partial buffers).
 struct GemmTile {
   int group, mt, nt, k0, k1;
   long long coff;

@@ -103,6 +103,8 @@ struct gbjk_ctx {
   int ws_nocc = -1;
   int wc_nocc = -1;
   int ksplit = 1;
+  bool narrow = false;  // half transform and fit on 64 x 16 tiles
+  bool elem_ht = false, elem_k = false;  // one thread per output (tiny problems)
   double *d_C = nullptr, *d_Cg = nullptr, *d_H = nullptr, *d_H2 = nullptr, *d_Kpart = nullptr,
          *d_K = nullptr;
   GemmGroup* d_groups = nullptr;
@@ -239,14 +241,22 @@ int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 // auxiliary rows per block of the mixed-path J column sums
 constexpr int kColsumChunk = 512;
 
+// Tiles of tm rows x tn columns: 64 x 64, 64 x 16 (narrow kernel) or
+// 16 x 16 (one thread per output).
 void add_tiles(std::vector<GemmTile>& tiles, int group, int M, int N, int k0, int k1,
-               long long coff, bool upper_only) {
-  for (int mt = 0; mt < cdiv(M, 64); ++mt)
-    for (int nt = 0; nt < cdiv(N, 64); ++nt) {
+               long long coff, bool upper_only, int tn = 64, int tm = 64) {
+  for (int mt = 0; mt < cdiv(M, tm); ++mt)
+    for (int nt = 0; nt < cdiv(N, tn); ++nt) {
       if (upper_only && nt < mt) continue;
       tiles.push_back({group, mt, nt, k0, k1, coff});
     }
 }
+
+// Occupied counts up to this many use 64 x 16 tiles in the FP64 half
+// transform and fit (a 64 x 64 tile would be mostly padding); a GEMM phase
+// with at most kElemOutputs outputs runs one thread per output instead.
+constexpr int kNarrowN = 16;
+constexpr long long kElemOutputs = 1 << 20;
 
 // Coefficient workspaces shared by both paths.
 gbjk_status ensure_c_workspace(gbjk_ctx* ctx, int nocc) {
@@ -283,6 +293,14 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
   gbjk_k_split_plan(ctx->nbf, ctx->naux, nocc, &ks, &kchunk64);
   ctx->ksplit = ks;
   if ((s = dalloc(ctx, &ctx->d_Kpart, (size_t)ks * nbf * nbf))) return s;
+  const bool elem_ht = (long long)nbf * naux * nocc <= kElemOutputs;
+  const bool elem_k = (long long)nbf * nbf * ks <= kElemOutputs;
+  const bool narrow = !elem_ht && nocc <= kNarrowN;
+  ctx->narrow = narrow;
+  ctx->elem_ht = elem_ht;
+  ctx->elem_k = elem_k;
+  const int ht_tm = elem_ht ? 16 : 64, ht_tn = elem_ht || narrow ? 16 : 64;
+  const int k_t = elem_k ? 16 : 64;
 
   std::vector<GemmGroup> groups;
   std::vector<GemmTile> tiles;
@@ -301,7 +319,7 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
     g.ldc = nocc;
     g.flags = 0;
     if (g.K == 0) continue;
-    add_tiles(tiles, (int)groups.size(), g.M, g.N, 0, g.K, 0, false);
+    add_tiles(tiles, (int)groups.size(), g.M, g.N, 0, g.K, 0, false, ht_tn, ht_tm);
     groups.push_back(g);
   }
   ctx->ht_ntiles = (int)tiles.size();
@@ -320,7 +338,7 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
     g.ldb = nocc;
     g.ldc = nocc;
     g.flags = kLowerA;
-    add_tiles(tiles, (int)groups.size(), g.M, g.N, 0, g.K, 0, false);
+    add_tiles(tiles, (int)groups.size(), g.M, g.N, 0, g.K, 0, false, ht_tn, ht_tm);
     groups.push_back(g);
   }
   ctx->fit_ntiles = (int)tiles.size() - ctx->fit_tile0;
@@ -358,7 +376,7 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
     for (int k = 0; k < ks; ++k) {
       const int k0 = k * kchunk, k1 = (int)std::min<long long>(kdim, (long long)(k + 1) * kchunk);
       add_tiles(tiles, ctx->syrk_group, g.M, g.N, k0, std::max(k0, k1), (long long)k * nbf * nbf,
-                true);
+                true, k_t, k_t);
     }
     ctx->syrk_ntiles = (int)tiles.size() - ctx->syrk_tile0;
   }
@@ -381,7 +399,7 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
     for (int k = 0; k < ks; ++k) {
       const int k0 = k * kchunk, k1 = (int)std::min<long long>(kdim, (long long)(k + 1) * kchunk);
       add_tiles(tiles, ctx->lmo_group, g.M, g.N, k0, std::max(k0, k1), (long long)k * nbf * nbf,
-                false);
+                false, k_t, k_t);
     }
     ctx->lmo_ntiles = (int)tiles.size() - ctx->lmo_tile0;
   }
@@ -413,13 +431,21 @@ gbjk_status ensure_j_workspace(gbjk_ctx* ctx) {
 }
 
 gbjk_status launch_gemm(gbjk_ctx* ctx, int tile0, int ntiles, bool transB, double alpha,
-                        int phase) {
+                        int phase, bool narrow = false, bool elem = false) {
   if (ntiles == 0) return GBJK_OK;
   PhaseScope ps(ctx, phase);
-  if (transB)
-    k_gemm_fp64<true><<<ntiles, 256, 0, ctx->stream>>>(ctx->d_groups, ctx->d_tiles + tile0, alpha);
+  const GemmGroup* g = ctx->d_groups;
+  const GemmTile* t = ctx->d_tiles + tile0;
+  if (elem && transB)
+    k_gemm_fp64_elem<true><<<ntiles, 256, 0, ctx->stream>>>(g, t, alpha);
+  else if (elem)
+    k_gemm_fp64_elem<false><<<ntiles, 256, 0, ctx->stream>>>(g, t, alpha);
+  else if (narrow)
+    k_gemm_fp64<false, false, 16><<<ntiles, 64, 0, ctx->stream>>>(g, t, alpha);
+  else if (transB)
+    k_gemm_fp64<true><<<ntiles, 256, 0, ctx->stream>>>(g, t, alpha);
   else
-    k_gemm_fp64<false><<<ntiles, 256, 0, ctx->stream>>>(ctx->d_groups, ctx->d_tiles + tile0, alpha);
+    k_gemm_fp64<false><<<ntiles, 256, 0, ctx->stream>>>(g, t, alpha);
   CKL(phase);
   return GBJK_OK;
 }
@@ -502,14 +528,17 @@ gbjk_status run_k(gbjk_ctx* ctx, int kmethod, const double* dC, int nocc, double
                                                              ctx->ncols_total, ctx->d_Cg);
     CKL(PH_GATHER);
   }
-  if ((s = launch_gemm(ctx, ctx->ht_tile0, ctx->ht_ntiles, false, 1.0, PH_HT))) return s;
+  if ((s = launch_gemm(ctx, ctx->ht_tile0, ctx->ht_ntiles, false, 1.0, PH_HT, ctx->narrow,
+                       ctx->elem_ht)))
+    return s;
   const bool mo = kmethod == GBJK_K_DFMO || ctx->fitted;
   if (!ctx->fitted &&
       (s = launch_gemm(ctx, mo ? ctx->fit_tile0 : ctx->fitV_tile0, ctx->fit_ntiles, false, 1.0,
-                       PH_FIT)))
+                       PH_FIT, ctx->narrow, ctx->elem_ht)))
     return s;
   if ((s = launch_gemm(ctx, mo ? ctx->syrk_tile0 : ctx->lmo_tile0,
-                       mo ? ctx->syrk_ntiles : ctx->lmo_ntiles, true, 1.0, PH_KGEMM)))
+                       mo ? ctx->syrk_ntiles : ctx->lmo_ntiles, true, 1.0, PH_KGEMM, false,
+                       ctx->elem_k)))
     return s;
   {
     PhaseScope ps(ctx, PH_KREDUCE);
@@ -531,7 +560,9 @@ gbjk_status gbjk_k_split_plan(int nbf, int naux, int nocc, int* ksplit, long lon
   const int nt = (nbf + 63) / 64;
   const int ntile_upper = nt * (nt + 1) / 2;
   int ks = std::max(1, std::min<int>(64, 4 * 152 / std::max(1, ntile_upper)));
-  while (ks > 1 && kdim / ks < 256) --ks;
+  // at least 64 k per part; tiny problems split further so that the few
+  // output tiles still spread over many SMs (the FP64 pipe is the bound)
+  while (ks > 1 && kdim / ks < 64) --ks;
   long long kc = ((kdim + ks - 1) / ks + 15) / 16 * 16;
   ks = (int)((kdim + kc - 1) / kc);
   *ksplit = ks;

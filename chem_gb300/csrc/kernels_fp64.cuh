@@ -273,19 +273,24 @@ __global__ void k_expand_panels(const double* __restrict__ P, const long long* _
       P[panel_off[I] + ((long long)m * naux + X) * KI + k];
 }
 
-// Grouped FP64 GEMM over a tile list; 64x64 tiles, 256 threads, 4x4 per thread.
+// Grouped FP64 GEMM over a tile list; 64 x TN tiles (TN = 64 or 16),
+// 16 * TN / 4 threads, 4x4 outputs per thread.  Every output is one in-order
+// fma chain over its k range, whatever the tile shape.
 // TRANSA: A is stored K x M row-major, op(A)(m, k) = A[k * lda + m].
-template <bool TRANSB, bool TRANSA = false>
-__global__ void __launch_bounds__(256)
+template <bool TRANSB, bool TRANSA = false, int TN = 64>
+__global__ void __launch_bounds__(TN * 4)
     k_gemm_fp64(const GemmGroup* __restrict__ groups, const GemmTile* __restrict__ tiles,
                 double alpha) {
+  static_assert(TN == 64 || TN == 16, "tile width");
+  constexpr int NT = TN * 4;   // threads
+  constexpr int CW = TN / 4;   // thread columns
   __shared__ double As[16][65];
-  __shared__ double Bs[16][65];
+  __shared__ double Bs[16][TN + 1];
   const GemmTile t = tiles[blockIdx.x];
   const GemmGroup g = groups[t.group];
   const int tid = threadIdx.x;
-  const int tx = tid & 15, ty = tid >> 4;
-  const int m0 = t.mt * 64, n0 = t.nt * 64;
+  const int tx = tid % CW, ty = tid / CW;
+  const int m0 = t.mt * 64, n0 = t.nt * TN;
   int kend = t.k1;
   if ((g.flags & kLowerA) && kend > m0 + 64) kend = m0 + 64;  // A[m][k] = 0 for k > m
   double acc[4][4];
@@ -295,8 +300,8 @@ __global__ void __launch_bounds__(256)
     for (int c = 0; c < 4; ++c) acc[r][c] = 0.0;
   for (int k0 = t.k0; k0 < kend; k0 += 16) {
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int idx = tid + 256 * r;
+    for (int r = 0; r < 1024 / NT; ++r) {
+      const int idx = tid + NT * r;
       if (TRANSA) {
         const int kk = idx >> 6, row = idx & 63;
         const int gm = m0 + row, gk = k0 + kk;
@@ -308,14 +313,14 @@ __global__ void __launch_bounds__(256)
       }
     }
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      const int idx = tid + 256 * r;
+    for (int r = 0; r < (16 * TN) / NT; ++r) {
+      const int idx = tid + NT * r;
       if (TRANSB) {
         const int col = idx >> 4, kk = idx & 15;
         const int gn = n0 + col, gk = k0 + kk;
         Bs[kk][col] = (gn < g.N && gk < kend) ? g.B[(long long)gn * g.ldb + gk] : 0.0;
       } else {
-        const int kk = idx >> 6, col = idx & 63;
+        const int kk = idx / TN, col = idx % TN;
         const int gn = n0 + col, gk = k0 + kk;
         Bs[kk][col] = (gn < g.N && gk < kend) ? g.B[(long long)gk * g.ldb + gn] : 0.0;
       }
@@ -327,7 +332,7 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int r = 0; r < 4; ++r) a[r] = As[kk][ty + 16 * r];
 #pragma unroll
-      for (int c = 0; c < 4; ++c) b[c] = Bs[kk][tx + 16 * c];
+      for (int c = 0; c < 4; ++c) b[c] = Bs[kk][tx + CW * c];
 #pragma unroll
       for (int r = 0; r < 4; ++r)
 #pragma unroll
@@ -342,13 +347,52 @@ __global__ void __launch_bounds__(256)
     if (gm >= g.M) continue;
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
-      const int gn = n0 + tx + 16 * c;
+      const int gn = n0 + tx + CW * c;
       if (gn >= g.N) continue;
       double v = alpha * acc[r][c];
       if (g.flags & kAccum) v += C[(long long)gm * g.ldc + gn];
       C[(long long)gm * g.ldc + gn] = v;
     }
   }
+}
+
+// Tiny problems: 16 x 16 tiles, one thread per output, each output the
+// in-order fma chain over the tile's k range read straight from global
+// memory.  A lower-triangular A stops at k = m: the terms beyond are exact
+// zeros, so every nonzero result equals the tiled kernel's bit for bit.
+// For problems so small that 64-row tiles would be mostly padding and the
+// few tiles would leave most SMs' FP64 units idle.
+template <bool TRANSB>
+__global__ void __launch_bounds__(256)
+    k_gemm_fp64_elem(const GemmGroup* __restrict__ groups, const GemmTile* __restrict__ tiles,
+                     double alpha) {
+  const GemmTile t = tiles[blockIdx.x];
+  const GemmGroup g = groups[t.group];
+  const int gm = t.mt * 16 + (threadIdx.x >> 4), gn = t.nt * 16 + (threadIdx.x & 15);
+  if (gm >= g.M || gn >= g.N) return;
+  int kend = t.k1;
+  if ((g.flags & kLowerA) && kend > gm + 1) kend = gm + 1;
+  const double* a = g.A + (long long)gm * g.lda;
+  const double* b = TRANSB ? g.B + (long long)gn * g.ldb : g.B + gn;
+  const long long bs = TRANSB ? 1 : g.ldb;
+  double acc = 0.0;
+  int k = t.k0;
+  // eight loads in flight, then their fmas in order
+  for (; k + 8 <= kend; k += 8) {
+    double av[8], bv[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      av[u] = a[k + u];
+      bv[u] = b[(long long)(k + u) * bs];
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc = fma(av[u], bv[u], acc);
+  }
+  for (; k < kend; ++k) acc = fma(a[k], b[(long long)k * bs], acc);
+  double* C = g.C + t.coff + (long long)gm * g.ldc + gn;
+  double v = alpha * acc;
+  if (g.flags & kAccum) v += *C;
+  *C = v;
 }
 
 // out[m][n] = alpha * sum_s part[s][m][n] over the upper triangle (n >= m)
