@@ -35,9 +35,16 @@ constexpr int kEriNW = (kEriLb + 1) * (kEriLb + 2) * (kEriLb + 3) / 6;          
 constexpr int kEriNcab = 36;  // (d cartesians)^2
 constexpr int kEriMaxSph = 7;
 constexpr int kEriWarps = 4;
-constexpr int kEriWarpDoubles = 2 * kEriNR + kEriNW * kEriMaxSph + 16;  // R x2, W, rn
+// Boys values (-2 alpha)^n F_n(T), n <= L, of up to kEriRnChunk (bra
+// primitive pair, auxiliary primitive) combinations, computed across the
+// lanes of a warp before the combinations are processed one by one
+constexpr int kEriRnChunk = 64;
+constexpr int kEriWarpDoubles =
+    2 * kEriNR + kEriNW * kEriMaxSph + kEriRnChunk * (kEriMaxL + 1);  // R x2, W, rn
 // cartesian -> spherical tables for l = 0..3, at offsets 0, 1, 10, 40
 __constant__ double c_eri_sph[1 + 9 + 30 + 70];
+// (t, u, v) of the compact Hermite index e (t + u + v <= 7): t | u << 8 | v << 16
+__constant__ int c_eri_tuv[kEriNR];
 
 struct EriShell {
   int l, nprim, prim0, bf_off;
@@ -122,6 +129,143 @@ __device__ void eri_hermite_pair(int la, int lb, double p, const double* PA, con
   }
 }
 
+// Compile-time forms of eri_idx's inverse and of the cartesian order.
+__host__ __device__ constexpr int eri_tuv_of(int e) {
+  int n = 0;
+  for (int sum = 0; sum <= kEriMaxL; ++sum)
+    for (int r = 0; r <= sum; ++r)
+      for (int v = 0; v <= r; ++v) {
+        if (n == e) return (sum - r) | ((r - v) << 8) | (v << 16);
+        ++n;
+      }
+  return 0;
+}
+__host__ __device__ constexpr int eri_cart_of(int l, int c) {
+  int idx = 0;
+  for (int ix = l; ix >= 0; --ix)
+    for (int iy = l - ix; iy >= 0; --iy) {
+      if (idx == c) return ix | (iy << 8) | ((l - ix - iy) << 16);
+      ++idx;
+    }
+  return 0;
+}
+__host__ __device__ constexpr int eri_idx_c(int t, int u, int v) {
+  return (t + u + v) * (t + u + v + 1) * (t + u + v + 2) / 6 + (u + v) * (u + v + 1) / 2 + v;
+}
+
+// An s-s AO shell pair against one auxiliary shell of angular momentum LC:
+// the lanes take the bra primitive pairs (the work of an s-s pair is all in
+// its primitives), each with its R table in registers; the partial sums of
+// the spherical auxiliary components end in acc of every lane (butterfly
+// sum).  Same terms as the general path, summed in another order.
+template <int LC>
+__device__ void eri_ss_aux(const double* pp, int psz, int npp, const EriShell& c,
+                           const double* __restrict__ ax_alpha,
+                           const double* __restrict__ ax_coef, int lane, double* acc) {
+  constexpr int NCC = (LC + 1) * (LC + 2) / 2, NSC = 2 * LC + 1;
+  constexpr int NR = (LC + 1) * (LC + 2) * (LC + 3) / 6;
+  const double* sc = c_eri_sph + (LC == 0 ? 0 : LC == 1 ? 1 : LC == 2 ? 10 : 40);
+  double part[NSC];
+#pragma unroll
+  for (int m = 0; m < NSC; ++m) part[m] = 0.0;
+  for (int q = lane; q < npp; q += 32) {
+    const double* o = pp + q * psz;
+    if (o[5] == 0.0) continue;
+    const double p = o[0];
+    double w[NSC];
+#pragma unroll
+    for (int m = 0; m < NSC; ++m) w[m] = 0.0;
+    for (int k = 0; k < c.nprim; ++k) {
+      const double qq = ax_alpha[c.prim0 + k];
+      const double alpha = p * qq / (p + qq);
+      const double pref = 2.0 * 17.493418327624862 / (p * qq * sqrt(p + qq)) * o[4] *
+                          ax_coef[c.prim0 + k];  // 2 pi^{5/2}
+      const double X = o[1] - c.A[0], Y = o[2] - c.A[1], Z = o[3] - c.A[2];
+      double F[LC + 1];
+      eri_boys(LC, alpha * (X * X + Y * Y + Z * Z), F);
+      double rn[LC + 1];
+      double fac = 1.0;
+#pragma unroll
+      for (int n = 0; n <= LC; ++n) {
+        rn[n] = fac * F[n];
+        fac *= -2.0 * alpha;
+      }
+      // R^n_{tuv} level by level, n = LC .. 0
+      double R[NR], Ro[NR];
+      R[0] = rn[LC];
+#pragma unroll
+      for (int n = LC - 1; n >= 0; --n) {
+#pragma unroll
+        for (int e = 0; e < NR; ++e) Ro[e] = R[e];
+#pragma unroll
+        for (int e = 0; e < NR; ++e) {
+          const int tuv = eri_tuv_of(e);
+          const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
+          if (t + u + v > LC - n) continue;
+          double val;
+          if (t > 0) {
+            val = X * Ro[eri_idx_c(t - 1, u, v)];
+            if (t > 1) val += (t - 1) * Ro[eri_idx_c(t - 2, u, v)];
+          } else if (u > 0) {
+            val = Y * Ro[eri_idx_c(t, u - 1, v)];
+            if (u > 1) val += (u - 1) * Ro[eri_idx_c(t, u - 2, v)];
+          } else if (v > 0) {
+            val = Z * Ro[eri_idx_c(t, u, v - 1)];
+            if (v > 1) val += (v - 1) * Ro[eri_idx_c(t, u, v - 2)];
+          } else {
+            val = rn[n];
+          }
+          R[e] = val;
+        }
+      }
+      // single-centre Hermite expansion of c
+      double Ec[LC + 1][LC + 2];
+#pragma unroll
+      for (int i = 0; i <= LC; ++i)
+#pragma unroll
+        for (int t = 0; t <= LC + 1; ++t) Ec[i][t] = 0.0;
+      Ec[0][0] = 1.0;
+      const double oo2q = 0.5 / qq;
+#pragma unroll
+      for (int i = 0; i < LC; ++i)
+#pragma unroll
+        for (int t = 0; t <= i + 1; ++t) {
+          double v = (t + 1 <= LC ? (t + 1) * Ec[i][t + 1] : 0.0);
+          if (t > 0) v += oo2q * Ec[i][t - 1];
+          Ec[i + 1][t] = v;
+        }
+#pragma unroll
+      for (int cc = 0; cc < NCC; ++cc) {
+        const int ex = eri_cart_of(LC, cc);
+        const int e0 = ex & 255, e1 = (ex >> 8) & 255, e2 = ex >> 16;
+        double s = 0.0;
+#pragma unroll
+        for (int tt = 0; tt <= e0; ++tt)
+#pragma unroll
+          for (int uu = 0; uu <= e1; ++uu)
+#pragma unroll
+            for (int vv = 0; vv <= e2; ++vv) {
+              const double sg = ((tt + uu + vv) & 1) ? -1.0 : 1.0;
+              s += sg * Ec[e0][tt] * Ec[e1][uu] * Ec[e2][vv] * R[eri_idx_c(tt, uu, vv)];
+            }
+        s *= pref;
+#pragma unroll
+        for (int mc = 0; mc < NSC; ++mc) w[mc] += sc[mc * NCC + cc] * s;
+      }
+    }
+    const double cf = o[6] * o[7] * o[8];  // E^{00} of the three axes
+#pragma unroll
+    for (int mc = 0; mc < NSC; ++mc) part[mc] += cf * w[mc];
+  }
+#pragma unroll
+  for (int mc = 0; mc < NSC; ++mc) {
+    double v = part[mc];
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    acc[mc] = v;
+  }
+}
+
 __global__ void __launch_bounds__(32 * kEriWarps)
     k_eri3c(const EriItem* __restrict__ items, const EriShell* __restrict__ ao,
             const EriShell* __restrict__ ax, const double* __restrict__ ao_alpha,
@@ -147,7 +291,7 @@ __global__ void __launch_bounds__(32 * kEriWarps)
   double* R0 = wbase;
   double* R1 = wbase + kEriNR;
   double* W = wbase + 2 * kEriNR;
-  double* rn = W + kEriNW * kEriMaxSph;
+  double* rnq = W + kEriNW * kEriMaxSph;  // kEriRnChunk x (kEriMaxL + 1)
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   // bra primitive pairs
@@ -190,7 +334,41 @@ __global__ void __launch_bounds__(32 * kEriWarps)
       const double* sc = c_eri_sph + eri_sph_off(lc);
       double acc0[kEriMaxSph], acc1[kEriMaxSph];  // cartesian pairs lane, lane + 32
       for (int m = 0; m < kEriMaxSph; ++m) acc0[m] = acc1[m] = 0.0;
-      for (int q = 0; q < npp; ++q) {
+      const int nck = c.nprim;
+      const int qch = kEriRnChunk / nck > 0 ? kEriRnChunk / nck : 1;
+      if (Lb == 0) {
+        // s-s pair: lanes over the bra primitive pairs; every lane ends
+        // with the sums, lane 0 stores them as the one cartesian pair
+        if (lc == 0)
+          eri_ss_aux<0>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+        else if (lc == 1)
+          eri_ss_aux<1>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+        else if (lc == 2)
+          eri_ss_aux<2>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+        else
+          eri_ss_aux<3>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+      }
+      for (int q0 = 0; q0 < (Lb == 0 ? 0 : npp); q0 += qch) {
+      const int q1 = min(npp, q0 + qch);
+      // Boys functions of the chunk's (q, k) combinations, one per lane
+      for (int jq = lane; jq < (q1 - q0) * nck; jq += 32) {
+        const int q = q0 + jq / nck, k = jq % nck;
+        const double* o = pp + q * psz;
+        if (o[5] == 0.0) continue;
+        const double p = o[0], qq = ax_alpha[c.prim0 + k];
+        const double alpha = p * qq / (p + qq);
+        const double X = o[1] - c.A[0], Y = o[2] - c.A[1], Z = o[3] - c.A[2];
+        double F[kEriMaxL + 1];
+        eri_boys(L, alpha * (X * X + Y * Y + Z * Z), F);
+        double fac = 1.0;
+        double* r = rnq + jq * (kEriMaxL + 1);
+        for (int n = 0; n <= L; ++n) {
+          r[n] = fac * F[n];
+          fac *= -2.0 * alpha;
+        }
+      }
+      __syncwarp();
+      for (int q = q0; q < q1; ++q) {
         const double* o = pp + q * psz;
         if (o[5] == 0.0) continue;
         const double p = o[0];
@@ -198,20 +376,10 @@ __global__ void __launch_bounds__(32 * kEriWarps)
         for (int m = 0; m < kEriMaxSph; ++m) w0[m] = w1[m] = 0.0;
         for (int k = 0; k < c.nprim; ++k) {
           const double qq = ax_alpha[c.prim0 + k];
-          const double alpha = p * qq / (p + qq);
           const double pref = 2.0 * 17.493418327624862 / (p * qq * sqrt(p + qq)) * o[4] *
                               ax_coef[c.prim0 + k];  // 2 pi^{5/2}
           const double X = o[1] - c.A[0], Y = o[2] - c.A[1], Z = o[3] - c.A[2];
-          if (lane == 0) {
-            double F[kEriMaxL + 1];
-            eri_boys(L, alpha * (X * X + Y * Y + Z * Z), F);
-            double fac = 1.0;
-            for (int n = 0; n <= L; ++n) {
-              rn[n] = fac * F[n];
-              fac *= -2.0 * alpha;
-            }
-          }
-          __syncwarp();
+          const double* rn = rnq + ((q - q0) * nck + k) * (kEriMaxL + 1);
           // R^n_{tuv}, levels n = L .. 0; level 0 ends in Rc
           double* cur = (L & 1) ? R1 : R0;
           double* old = (L & 1) ? R0 : R1;
@@ -223,12 +391,8 @@ __global__ void __launch_bounds__(32 * kEriWarps)
             old = t_;
             const int lt = L - n, cnt = eri_tet(lt + 1);
             for (int e = lane; e < cnt; e += 32) {
-              // decode e -> (t, u, v), t + u + v <= lt
-              int sidx = 0;
-              while (eri_tet(sidx + 1) <= e) ++sidx;
-              int rem = e - eri_tet(sidx), r = 0;
-              while ((r + 1) * (r + 2) / 2 <= rem) ++r;
-              const int v = rem - r * (r + 1) / 2, u = r - v, t = sidx - r;
+              const int tuv = c_eri_tuv[e];
+              const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
               double val;
               if (t > 0) {
                 val = X * old[eri_idx(t - 1, u, v)];
@@ -263,11 +427,8 @@ __global__ void __launch_bounds__(32 * kEriWarps)
           for (int h = 0; h < 2; ++h) {
             const int e = lane + 32 * h;
             if (e >= nW) break;
-            int sidx = 0;
-            while (eri_tet(sidx + 1) <= e) ++sidx;
-            int rem = e - eri_tet(sidx), r = 0;
-            while ((r + 1) * (r + 2) / 2 <= rem) ++r;
-            const int v = rem - r * (r + 1) / 2, u = r - v, t = sidx - r;
+            const int tuv = c_eri_tuv[e];
+            const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
             for (int cc = 0; cc < ncc; ++cc) {
               int ex[3];
               eri_cart(lc, cc, ex);
@@ -325,6 +486,8 @@ __global__ void __launch_bounds__(32 * kEriWarps)
           }
         }
         __syncwarp();
+      }
+      __syncwarp();  // the next chunk rewrites the Boys values
       }
       // spherical (a, b): stage the cartesian accumulators in the warp's
       // R/W space, then each lane writes outputs (ma, mb, mc)

@@ -780,10 +780,17 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
   for (int s = 0; s < ao->nshell; ++s)
     if (ao->l[s] < 0 || ao->l[s] > kEriMaxLao)
       return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_eri3c: AO shells above d are not supported");
-  for (int s = 0; s < aux->nshell; ++s)
+  for (int s = 0; s < aux->nshell; ++s) {
     if (aux->l[s] < 0 || aux->l[s] > kEriMaxLaux)
       return fail(ctx, GBJK_INVALID_ARG,
                   "gbjk_upload_b_eri3c: auxiliary shells above f are not supported");
+    if (aux->nprim[s] < 1 || aux->nprim[s] > kEriRnChunk)
+      return fail(ctx, GBJK_INVALID_ARG,
+                  "gbjk_upload_b_eri3c: auxiliary contraction length out of range");
+  }
+  for (int s = 0; s < ao->nshell; ++s)
+    if (ao->nprim[s] < 1)
+      return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_eri3c: empty AO contraction");
   CK(cudaSetDevice(ctx->device));
   // host-side tables: shells, primitives, work items (AO shell pairs)
   auto shells = [](const gbjk_shells* b, std::vector<EriShell>& out) {
@@ -847,6 +854,14 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
   if (!e) e = up(col_IJ, (size_t)npairs * 4, &d_cij);
   if (!e) e = up(col_JI, (size_t)npairs * 4, &d_cji);
   if (!e) e = cudaMemcpyToSymbol(c_eri_sph, sph, sizeof(double) * (1 + 9 + 30 + 70));
+  if (!e) {
+    // compact Hermite index -> (t, u, v), in the order of eri_idx
+    int tuv[kEriNR], n = 0;
+    for (int sum = 0; sum <= kEriMaxL; ++sum)
+      for (int r = 0; r <= sum; ++r)
+        for (int v = 0; v <= r; ++v) tuv[n++] = (sum - r) | ((r - v) << 8) | (v << 16);
+    e = cudaMemcpyToSymbol(c_eri_tuv, tuv, sizeof(tuv));
+  }
   if (!e) e = cudaFuncSetAttribute(k_eri3c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (!e && !items.empty()) {
     {
