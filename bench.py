@@ -43,6 +43,9 @@ def parse():
     ap.add_argument("--no-scf", action="store_true")
     ap.add_argument("--no-dfao", action="store_true")
     ap.add_argument("--no-water", action="store_true")
+    ap.add_argument("--device-setup", action="store_true",
+                    help="serving: add a set-up worker that computes the 3-center "
+                         "integrals on the GPU")
     ap.add_argument("--workload", default="fock", choices=["fock", "serving", "synthetic", "mp2"])
     ap.add_argument("--mp2-alkane", type=int, default=40)
     ap.add_argument("--mp2-points", type=int, default=8)
@@ -290,7 +293,8 @@ def run_serving(args):
                   file=sys.stderr, flush=True)
 
     srv = FockServer(budget_bytes=args.budget_gb * 1e9, slots=args.slots,
-                     precision=args.precision, progress=progress)
+                     precision=args.precision, progress=progress,
+                     device_setup=args.device_setup)
     t0 = time.perf_counter()
     with ClockSampler(0) as clk:
         done = srv.run(reqs)
@@ -309,7 +313,10 @@ def run_serving(args):
                                f"alkanes C4..C{args.alkane_max}, (H2O)2..{args.water_max}, "
                                "cc-pVDZ/cc-pVDZ-jkfit", "budget_gb": args.budget_gb,
                    "slots": args.slots, "precision": args.precision,
-                   "distinct_molecules": len(set(q.key for q in reqs))},
+                   "distinct_molecules": len(set(q.key for q in reqs)),
+                   "setup": "host and device integral workers on one queue"
+                            if args.device_setup else "host integrals"},
+        "setup_routes": {r: len({q.key for q in done if q.route == r}) for r in ("host", "device")},
         "latency_arrival_to_result": latency_stats(ok),
         "latency_service": {"p50_s": float(np.percentile(svc, 50)),
                             "p99_s": float(np.percentile(svc, 99)),

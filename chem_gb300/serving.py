@@ -8,7 +8,11 @@ workspaces) and serves requests as they arrive:
 * set-up — the host integrals of a molecule not seen before run on a CPU
   pipeline (one job at a time, each using all host threads), shortest
   estimated job first (a request's `cost` hint; arrival order without one),
-  except that a job waiting longer than `max_setup_wait` goes first;
+  except that a job waiting longer than `max_setup_wait` goes first; with
+  `device_setup`, a second worker takes jobs from the same queue and sets
+  its molecule up with the 3-center integrals computed on the GPU
+  (gbjk_upload_b_eri3c) while it admits the engine, so host and device
+  integrals run side by side (the route taken is recorded on the request);
 * admission — a molecule's engine is created when its device footprint fits
   the HBM budget; idle engines are evicted to make room, first those with
   no requests waiting (least-recently-used first), then any idle one;
@@ -44,6 +48,10 @@ class Request:
     arrival: float       # seconds after the start of the run
     make_system: object  # callable() -> (DFSystem, P_alpha, C_occ)
     cost: float = None   # relative set-up cost estimate (shortest job first)
+    # callable() -> the same without the host 3-center tensor (B left to the
+    # device engine); used by the device set-up worker
+    make_system_device: object = None
+    route: str = None    # "host" or "device": how the molecule was set up
     t_setup_done: float = None
     t_admitted: float = None
     t_done: float = None
@@ -86,8 +94,11 @@ class FockServer:
 
     def __init__(self, budget_bytes=150e9, slots=4, precision="split", device=0,
                  engine_factory=None, clock=time.perf_counter, drop_host_tensor=True,
-                 max_host_bytes=48e9, progress=None, max_setup_wait=60.0):
+                 max_host_bytes=48e9, progress=None, max_setup_wait=60.0,
+                 device_setup=False):
         self.budget = int(budget_bytes)
+        self.device_setup = device_setup
+        self._routes = {}                # key -> "host" | "device"
         self.drop_host_tensor = drop_host_tensor
         self.max_host_bytes = int(max_host_bytes)
         self.progress = progress  # callable(done, total) after each request
@@ -200,7 +211,7 @@ class FockServer:
                 self._host_bytes[req.key] = int(ds.B.nbytes)
                 self._host_pending += int(ds.B.nbytes)
         eng = self._engine_factory(ds)
-        if self.drop_host_tensor and getattr(ds, "B", None) is not None:
+        if self.drop_host_tensor and isinstance(getattr(ds, "B", None), np.ndarray):
             ds.B = None  # the engine holds the device copy
             with self._cv:
                 self._host_pending -= self._host_bytes.pop(req.key, 0)
@@ -246,6 +257,39 @@ class FockServer:
                 self._systems[req.key] = sysm
                 self._host_pending += nb
                 self._host_bytes[req.key] = nb
+
+    def _setup_device(self, req):
+        """Device route: the host part of the set-up (screening, metric) on
+        this thread, then admission of the molecule's engine, whose
+        3-center tensor the GPU computes; the engine becomes resident and
+        idle, ready for the molecule's requests."""
+        if req.key not in self._systems:
+            sysm = req.make_system_device()
+            with self._cv:
+                self._systems[req.key] = sysm
+        ds = self._systems[req.key][0]
+        need = footprint_bytes(ds.layout, ds.nocc, self.precision)
+        if need > self.budget:
+            raise RuntimeError(f"molecule {req.key} needs {need / 1e9:.1f} GB > budget")
+        with self._cv:
+            self._admitting.add(req.key)
+            while not self._evict_for(need):
+                self._cv.wait()
+            self._used += need
+            self.max_used = max(self.max_used, self._used)
+        try:
+            eng = self._engine_factory(ds)
+        except BaseException:
+            with self._cv:
+                self._used -= need
+                self._admitting.discard(req.key)
+                self._cv.notify_all()
+            raise
+        with self._cv:
+            self._resident[req.key] = _Resident(eng, need)
+            self._admitting.discard(req.key)
+            self.log.append(("admit", req.key))
+            self._cv.notify_all()
 
     def _on_setup(self, req, t0):
         req.t_setup_done = self.clock() - t0
@@ -297,7 +341,7 @@ class FockServer:
                                                  else 0.0, jobs[i][1]))
         return jobs.pop(i)[0]
 
-    def _setup_loop(self, t0, total):
+    def _setup_loop(self, t0, total, route="host"):
         while True:
             with self._cv:
                 while not self._setup_jobs and not self._submitted_all:
@@ -305,15 +349,22 @@ class FockServer:
                 if not self._setup_jobs:
                     return
                 req = self._next_setup(self.clock())
+            how = "device" if route == "device" and req.make_system_device is not None else "host"
+            with self._cv:
+                self._routes[req.key] = how
             err = None
             try:
-                self._setup(req)
+                if how == "device":
+                    self._setup_device(req)
+                else:
+                    self._setup(req)
             except Exception as e:  # recorded on every request of the molecule
                 err = f"set-up failed: {e}"
             with self._cv:
                 self._setup_done.add(req.key)
                 waiters = self._setup_waiters.pop(req.key, [])
             for q in waiters:
+                q.route = how
                 if err is None:
                     self._on_setup(q, t0)
                 else:
@@ -342,6 +393,7 @@ class FockServer:
                     self._setup_jobs.append((req, self.clock()))
                     self._cv.notify_all()
                 return
+        req.route = self._routes.get(req.key)
         if ok:
             self._on_setup(req, t0)
         else:
@@ -358,8 +410,11 @@ class FockServer:
         t0 = self.clock()
         workers = [threading.Thread(target=self._worker, args=(t0, len(reqs)), daemon=True)
                    for _ in range(self.slots)]
-        setup = threading.Thread(target=self._setup_loop, args=(t0, len(reqs)), daemon=True)
-        for w in workers + [setup]:
+        setups = [threading.Thread(target=self._setup_loop, args=(t0, len(reqs)), daemon=True)]
+        if self.device_setup:
+            setups.append(threading.Thread(target=self._setup_loop,
+                                           args=(t0, len(reqs), "device"), daemon=True))
+        for w in workers + setups:
             w.start()
         for req in reqs:
             if realtime:
@@ -370,8 +425,7 @@ class FockServer:
         with self._cv:
             self._submitted_all = True
             self._cv.notify_all()
-        setup.join()
-        for w in workers:
+        for w in setups + workers:
             w.join()
         return reqs
 
@@ -391,11 +445,13 @@ def latency_stats(requests):
             "mean_s": float(lat.mean()), "max_s": float(lat.max()), "n": int(lat.size)}
 
 
-def make_system_factory(kind, size, eps=1e-10, basis="cc-pvdz", dfbasis="cc-pvdz-jkfit"):
+def make_system_factory(kind, size, eps=1e-10, basis="cc-pvdz", dfbasis="cc-pvdz-jkfit",
+                        device_ints=False):
     """Callable building (DFSystem, P_alpha, C_occ) for an alkane C_nH_{2n+2}
     (kind 'alkane', size n) or a water cluster (kind 'water', size k) at the
     core-guess density.  Water-cluster geometries are seeded by k, so
-    requests of one cluster size share the molecule (and its set-up)."""
+    requests of one cluster size share the molecule (and its set-up).  With
+    device_ints the 3-center tensor is left to the device engine."""
     def make():
         from . import geometry
         from .dfsystem import build_dfsystem
@@ -404,7 +460,8 @@ def make_system_factory(kind, size, eps=1e-10, basis="cc-pvdz", dfbasis="cc-pvdz
             s, x = geometry.alkane(size)
         else:
             s, x = geometry.water_cluster(size, np.random.default_rng(1000 + size))
-        ds = build_dfsystem(molecule_from_angstrom(s, x, basis, dfbasis), eps=eps)
+        ds = build_dfsystem(molecule_from_angstrom(s, x, basis, dfbasis), eps=eps,
+                            device_ints=device_ints)
         sv, U = np.linalg.eigh(ds.S)
         X = U @ np.diag(sv ** -0.5) @ U.T
         _, Cp = np.linalg.eigh(X.T @ ds.Hcore @ X)
@@ -431,5 +488,6 @@ def poisson_requests(n, rate, seed, alkane=(4, 40), water=(2, 32)):
         # set-up cost grows ~ nbf^3 (3-center integrals with screening)
         nbf = 24 * size + 10 if kind == "alkane" else 24 * size
         out.append(Request(rid, f"{kind}{size}", t, make_system_factory(kind, size),
-                           cost=float(nbf) ** 3))
+                           cost=float(nbf) ** 3,
+                           make_system_device=make_system_factory(kind, size, device_ints=True)))
     return out

@@ -131,3 +131,46 @@ def test_setup_runs_shortest_job_first_and_failures_do_not_hang():
     assert done[2].error and "set-up failed" in done[2].error
     assert all(q.error is None for q in done if q.key != "bad")
     assert all(q.t_done is not None for q in done)
+
+
+def test_device_setup_worker_shares_the_queue():
+    # two set-up workers (host integrals, device integrals) drain one queue;
+    # each molecule keeps the route it was set up by, also when its engine
+    # is evicted and admitted again
+    created = []
+
+    def factory(ds):
+        created.append((ds.key, ds.B))
+        return _FakeEngine(ds)
+
+    def make(key, n, device):
+        def f():
+            time.sleep(0.02)
+            d = _DS(n, 200, 5)
+            d.key = key
+            d.B = ("device_ints", key) if device else np.zeros(4)
+            return d, np.eye(n), np.ones((n, 5))
+        return f
+
+    sizes = {f"m{i}": 40 + 2 * i for i in range(8)}
+    fp = max(footprint_bytes(_DS(n, 200, 5).layout, 5) for n in sizes.values())
+    reqs = []
+    for i in range(32):
+        key = f"m{i % 8}"
+        n = sizes[key]
+        reqs.append(Request(i, key, 0.0, make(key, n, False), cost=float(n),
+                            make_system_device=make(key, n, True)))
+    srv = FockServer(budget_bytes=3 * fp, slots=2, engine_factory=factory, device_setup=True,
+                     drop_host_tensor=True)
+    done = srv.run(reqs, realtime=False)
+    srv.close()
+    assert all(q.error is None for q in done), [q.error for q in done if q.error]
+    routes = {}
+    for q in done:
+        assert q.route in ("host", "device")
+        assert routes.setdefault(q.key, q.route) == q.route
+    assert set(routes.values()) == {"host", "device"}
+    assert srv.max_used <= 3 * fp
+    assert any(e[0] == "evict" for e in srv.log)
+    for key, B in created:
+        assert isinstance(B, tuple) == (routes[key] == "device"), (key, B)
