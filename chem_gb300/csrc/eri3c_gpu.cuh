@@ -39,12 +39,19 @@ constexpr int kEriWarps = 4;
 // primitive pair, auxiliary primitive) combinations, computed across the
 // lanes of a warp before the combinations are processed one by one
 constexpr int kEriRnChunk = 64;
-constexpr int kEriWarpDoubles =
-    2 * kEriNR + kEriNW * kEriMaxSph + kEriRnChunk * (kEriMaxL + 1);  // R x2, W, rn
+// ket matrix M[mc][j] of an auxiliary primitive: j over the Hermite
+// indices of t + u + v <= l_aux (at most 20), mc over its spherical components
+constexpr int kEriNKet = (kEriMaxLaux + 1) * (kEriMaxLaux + 2) * (kEriMaxLaux + 3) / 6;  // 20
+constexpr int kEriWarpDoubles = 2 * kEriNR + kEriNW * kEriMaxSph +
+                                kEriRnChunk * (kEriMaxL + 1) +
+                                kEriMaxSph * kEriNKet;  // R x2, W, rn, M
 // cartesian -> spherical tables for l = 0..3, at offsets 0, 1, 10, 40
 __constant__ double c_eri_sph[1 + 9 + 30 + 70];
 // (t, u, v) of the compact Hermite index e (t + u + v <= 7): t | u << 8 | v << 16
 __constant__ int c_eri_tuv[kEriNR];
+// 1 / (2 j + 1) for the Boys series and recursion (no FP64 division there)
+constexpr int kEriBoysTerms = 400;
+__constant__ double c_eri_rodd[kEriMaxL + kEriBoysTerms + 1];
 
 struct EriShell {
   int l, nprim, prim0, bf_off;
@@ -75,10 +82,13 @@ __device__ __forceinline__ void eri_cart(int l, int c, int* ex) {
     }
 }
 
-// Boys function F_0..F_n at T (same algorithm as the host engine).
+// Boys function F_0..F_n at T: the host engine's algorithm (series at
+// n = nmax and downward recursion, or erf and upward recursion for large T),
+// with the divisions by odd integers taken as products with their
+// reciprocals (a rounding-level difference from the host).
 __device__ void eri_boys(int nmax, double T, double* F) {
   if (T < 1e-15) {
-    for (int m = 0; m <= nmax; ++m) F[m] = 1.0 / (2 * m + 1);
+    for (int m = 0; m <= nmax; ++m) F[m] = c_eri_rodd[m];
     return;
   }
   const double eT = exp(-T);
@@ -88,18 +98,51 @@ __device__ void eri_boys(int nmax, double T, double* F) {
     for (int m = 0; m < nmax; ++m) F[m + 1] = ((2 * m + 1) * F[m] - eT) * inv2T;
     return;
   }
-  double denom = 2 * nmax + 1;
-  double term = 1.0 / denom;
+  double term = c_eri_rodd[nmax];
   double sum = term;
   const double twoT = 2.0 * T;
-  for (int k = 1; k < 400; ++k) {
-    denom += 2.0;
-    term *= twoT / denom;
+  for (int k = 1; k < kEriBoysTerms; ++k) {
+    term *= twoT * c_eri_rodd[nmax + k];
     sum += term;
     if (term < 1e-17 * sum) break;
   }
   F[nmax] = eT * sum;
-  for (int m = nmax - 1; m >= 0; --m) F[m] = (twoT * F[m + 1] + eT) / (2 * m + 1);
+  for (int m = nmax - 1; m >= 0; --m) F[m] = (twoT * F[m + 1] + eT) * c_eri_rodd[m];
+}
+
+// Ket matrix of an auxiliary primitive of exponent qq and angular momentum
+// lc, computed across the lanes of a warp into M (row stride kEriNKet):
+//   M[mc][j] = (-1)^(t+u+v) sum_cc sph[mc][cc] Ec[cx][t] Ec[cy][u] Ec[cz][v],
+// (t, u, v) the Hermite index j, (cx, cy, cz) the cartesian exponents of cc,
+// Ec the single-centre Hermite expansion.  The contraction with the R table
+// is then W[tuv][mc] = pref sum_j M[mc][j] R[(t, u, v) + j].
+__device__ void eri_ket_matrix(int lc, double qq, int lane, double* M) {
+  double Ec[kEriMaxLaux + 1][kEriMaxLaux + 2];
+  for (int i = 0; i <= kEriMaxLaux; ++i)
+    for (int t = 0; t <= kEriMaxLaux + 1; ++t) Ec[i][t] = 0.0;
+  Ec[0][0] = 1.0;
+  const double oo2q = 0.5 / qq;
+  for (int i = 0; i < lc; ++i)
+    for (int t = 0; t <= i + 1; ++t) {
+      double v = (t + 1) * Ec[i][t + 1];
+      if (t > 0) v += oo2q * Ec[i][t - 1];
+      Ec[i + 1][t] = v;
+    }
+  const int ncc = (lc + 1) * (lc + 2) / 2, nsc = 2 * lc + 1, nr = eri_tet(lc + 1);
+  const double* sc = c_eri_sph + eri_sph_off(lc);
+  for (int en = lane; en < nsc * nr; en += 32) {
+    const int mc = en / nr, j = en % nr;
+    const int tuv = c_eri_tuv[j];
+    const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
+    double m = 0.0;
+    for (int cc = 0; cc < ncc; ++cc) {
+      int ex[3];
+      eri_cart(lc, cc, ex);
+      if (t > ex[0] || u > ex[1] || v > ex[2]) continue;
+      m += sc[mc * ncc + cc] * (Ec[ex[0]][t] * Ec[ex[1]][u] * Ec[ex[2]][v]);
+    }
+    M[mc * kEriNKet + j] = ((t + u + v) & 1) ? -m : m;
+  }
 }
 
 // E[axis][i][j][t] of one primitive pair, i <= la, j <= lb, t <= i + j, in
@@ -155,28 +198,30 @@ __host__ __device__ constexpr int eri_idx_c(int t, int u, int v) {
 
 // An s-s AO shell pair against one auxiliary shell of angular momentum LC:
 // the lanes take the bra primitive pairs (the work of an s-s pair is all in
-// its primitives), each with its R table in registers; the partial sums of
-// the spherical auxiliary components end in acc of every lane (butterfly
-// sum).  Same terms as the general path, summed in another order.
+// its primitives), each with its R table in registers; per auxiliary
+// primitive the warp first builds the ket matrix M (shared memory), then
+// W[mc] = pref sum_j M[mc][j] R[j].  The partial sums of the spherical
+// auxiliary components end in acc of every lane (butterfly sum).  Same
+// terms as the general path, summed in another order.
 template <int LC>
 __device__ void eri_ss_aux(const double* pp, int psz, int npp, const EriShell& c,
                            const double* __restrict__ ax_alpha,
-                           const double* __restrict__ ax_coef, int lane, double* acc) {
-  constexpr int NCC = (LC + 1) * (LC + 2) / 2, NSC = 2 * LC + 1;
+                           const double* __restrict__ ax_coef, int lane, double* M,
+                           double* acc) {
+  constexpr int NSC = 2 * LC + 1;
   constexpr int NR = (LC + 1) * (LC + 2) * (LC + 3) / 6;
-  const double* sc = c_eri_sph + (LC == 0 ? 0 : LC == 1 ? 1 : LC == 2 ? 10 : 40);
   double part[NSC];
 #pragma unroll
   for (int m = 0; m < NSC; ++m) part[m] = 0.0;
-  for (int q = lane; q < npp; q += 32) {
-    const double* o = pp + q * psz;
-    if (o[5] == 0.0) continue;
-    const double p = o[0];
-    double w[NSC];
-#pragma unroll
-    for (int m = 0; m < NSC; ++m) w[m] = 0.0;
-    for (int k = 0; k < c.nprim; ++k) {
-      const double qq = ax_alpha[c.prim0 + k];
+  for (int k = 0; k < c.nprim; ++k) {
+    const double qq = ax_alpha[c.prim0 + k];
+    __syncwarp();  // the previous primitive's M is no longer read
+    eri_ket_matrix(LC, qq, lane, M);
+    __syncwarp();
+    for (int q = lane; q < npp; q += 32) {
+      const double* o = pp + q * psz;
+      if (o[5] == 0.0) continue;
+      const double p = o[0];
       const double alpha = p * qq / (p + qq);
       const double pref = 2.0 * 17.493418327624862 / (p * qq * sqrt(p + qq)) * o[4] *
                           ax_coef[c.prim0 + k];  // 2 pi^{5/2}
@@ -218,44 +263,15 @@ __device__ void eri_ss_aux(const double* pp, int psz, int npp, const EriShell& c
           R[e] = val;
         }
       }
-      // single-centre Hermite expansion of c
-      double Ec[LC + 1][LC + 2];
+      const double cf = o[6] * o[7] * o[8] * pref;  // E^{00} of the three axes
 #pragma unroll
-      for (int i = 0; i <= LC; ++i)
+      for (int mc = 0; mc < NSC; ++mc) {
+        double w = 0.0;
 #pragma unroll
-        for (int t = 0; t <= LC + 1; ++t) Ec[i][t] = 0.0;
-      Ec[0][0] = 1.0;
-      const double oo2q = 0.5 / qq;
-#pragma unroll
-      for (int i = 0; i < LC; ++i)
-#pragma unroll
-        for (int t = 0; t <= i + 1; ++t) {
-          double v = (t + 1 <= LC ? (t + 1) * Ec[i][t + 1] : 0.0);
-          if (t > 0) v += oo2q * Ec[i][t - 1];
-          Ec[i + 1][t] = v;
-        }
-#pragma unroll
-      for (int cc = 0; cc < NCC; ++cc) {
-        const int ex = eri_cart_of(LC, cc);
-        const int e0 = ex & 255, e1 = (ex >> 8) & 255, e2 = ex >> 16;
-        double s = 0.0;
-#pragma unroll
-        for (int tt = 0; tt <= e0; ++tt)
-#pragma unroll
-          for (int uu = 0; uu <= e1; ++uu)
-#pragma unroll
-            for (int vv = 0; vv <= e2; ++vv) {
-              const double sg = ((tt + uu + vv) & 1) ? -1.0 : 1.0;
-              s += sg * Ec[e0][tt] * Ec[e1][uu] * Ec[e2][vv] * R[eri_idx_c(tt, uu, vv)];
-            }
-        s *= pref;
-#pragma unroll
-        for (int mc = 0; mc < NSC; ++mc) w[mc] += sc[mc * NCC + cc] * s;
+        for (int jj = 0; jj < NR; ++jj) w += M[mc * kEriNKet + jj] * R[jj];
+        part[mc] += cf * w;
       }
     }
-    const double cf = o[6] * o[7] * o[8];  // E^{00} of the three axes
-#pragma unroll
-    for (int mc = 0; mc < NSC; ++mc) part[mc] += cf * w[mc];
   }
 #pragma unroll
   for (int mc = 0; mc < NSC; ++mc) {
@@ -266,7 +282,7 @@ __device__ void eri_ss_aux(const double* pp, int psz, int npp, const EriShell& c
   }
 }
 
-__global__ void __launch_bounds__(32 * kEriWarps)
+__global__ void __launch_bounds__(32 * kEriWarps, 4)
     k_eri3c(const EriItem* __restrict__ items, const EriShell* __restrict__ ao,
             const EriShell* __restrict__ ax, const double* __restrict__ ao_alpha,
             const double* __restrict__ ao_coef, const double* __restrict__ ax_alpha,
@@ -292,6 +308,7 @@ __global__ void __launch_bounds__(32 * kEriWarps)
   double* R1 = wbase + kEriNR;
   double* W = wbase + 2 * kEriNR;
   double* rnq = W + kEriNW * kEriMaxSph;  // kEriRnChunk x (kEriMaxL + 1)
+  double* Mk = rnq + kEriRnChunk * (kEriMaxL + 1);  // kEriMaxSph x kEriNKet
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 
   // bra primitive pairs
@@ -329,9 +346,8 @@ __global__ void __launch_bounds__(32 * kEriWarps)
     for (int s = ablk_shell_off[A]; s < ablk_shell_off[A + 1]; ++s, ++counter) {
       if (counter % kEriWarps != warp) continue;
       const EriShell c = ax[s];
-      const int lc = c.l, ncc = (lc + 1) * (lc + 2) / 2, nsc = 2 * lc + 1;
+      const int lc = c.l, nsc = 2 * lc + 1;
       const int L = Lb + lc;
-      const double* sc = c_eri_sph + eri_sph_off(lc);
       double acc0[kEriMaxSph], acc1[kEriMaxSph];  // cartesian pairs lane, lane + 32
       for (int m = 0; m < kEriMaxSph; ++m) acc0[m] = acc1[m] = 0.0;
       const int nck = c.nprim;
@@ -340,13 +356,17 @@ __global__ void __launch_bounds__(32 * kEriWarps)
         // s-s pair: lanes over the bra primitive pairs; every lane ends
         // with the sums, lane 0 stores them as the one cartesian pair
         if (lc == 0)
-          eri_ss_aux<0>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+          eri_ss_aux<0>(pp, psz, npp, c, ax_alpha, ax_coef, lane, Mk, acc0);
         else if (lc == 1)
-          eri_ss_aux<1>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+          eri_ss_aux<1>(pp, psz, npp, c, ax_alpha, ax_coef, lane, Mk, acc0);
         else if (lc == 2)
-          eri_ss_aux<2>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+          eri_ss_aux<2>(pp, psz, npp, c, ax_alpha, ax_coef, lane, Mk, acc0);
         else
-          eri_ss_aux<3>(pp, psz, npp, c, ax_alpha, ax_coef, lane, acc0);
+          eri_ss_aux<3>(pp, psz, npp, c, ax_alpha, ax_coef, lane, Mk, acc0);
+      } else if (nck == 1) {
+        // one auxiliary primitive: its ket matrix serves every bra pair
+        eri_ket_matrix(lc, ax_alpha[c.prim0], lane, Mk);
+        __syncwarp();
       }
       for (int q0 = 0; q0 < (Lb == 0 ? 0 : npp); q0 += qch) {
       const int q1 = min(npp, q0 + qch);
@@ -411,45 +431,23 @@ __global__ void __launch_bounds__(32 * kEriWarps)
             __syncwarp();
           }
           const double* Rc = cur;
-          // single-centre Hermite expansion of c: Ec[i][t], i <= lc
-          double Ec[4][4];
-          for (int i = 0; i < 4; ++i)
-            for (int t = 0; t < 4; ++t) Ec[i][t] = 0.0;
-          Ec[0][0] = 1.0;
-          const double oo2q = 0.5 / qq;
-          for (int i = 0; i < lc; ++i)
-            for (int t = 0; t <= i + 1; ++t) {
-              double v = (t + 1 <= 3 ? (t + 1) * Ec[i][t + 1] : 0.0);
-              if (t > 0) v += oo2q * Ec[i][t - 1];
-              Ec[i + 1][t] = v;
-            }
-          // W[tuv][mc] += pref sum_cc sph[mc][cc] sum_ket sign E R
+          // W[tuv][mc] += pref sum_j M[mc][j] R[(t, u, v) + j]
+          if (nck > 1) {
+            eri_ket_matrix(lc, qq, lane, Mk);
+            __syncwarp();
+          }
+          const int nr = eri_tet(lc + 1);
           for (int h = 0; h < 2; ++h) {
             const int e = lane + 32 * h;
             if (e >= nW) break;
             const int tuv = c_eri_tuv[e];
             const int t = tuv & 255, u = (tuv >> 8) & 255, v = tuv >> 16;
-            for (int cc = 0; cc < ncc; ++cc) {
-              int ex[3];
-              eri_cart(lc, cc, ex);
-              double s = 0.0;
-              for (int tt = 0; tt <= ex[0]; ++tt) {
-                const double e1 = Ec[ex[0]][tt];
-                if (e1 == 0.0) continue;
-                for (int uu = 0; uu <= ex[1]; ++uu) {
-                  const double e2 = Ec[ex[1]][uu];
-                  if (e2 == 0.0) continue;
-                  for (int vv = 0; vv <= ex[2]; ++vv) {
-                    const double e3 = Ec[ex[2]][vv];
-                    if (e3 == 0.0) continue;
-                    const double sg = ((tt + uu + vv) & 1) ? -1.0 : 1.0;
-                    s += sg * e1 * e2 * e3 * Rc[eri_idx(t + tt, u + uu, v + vv)];
-                  }
-                }
-              }
-              s *= pref;
-              double* w = h ? w1 : w0;
-              for (int mc = 0; mc < nsc; ++mc) w[mc] += sc[mc * ncc + cc] * s;
+            double* w = h ? w1 : w0;
+            for (int jj = 0; jj < nr; ++jj) {
+              const int kt = c_eri_tuv[jj];
+              const double r =
+                  pref * Rc[eri_idx(t + (kt & 255), u + ((kt >> 8) & 255), v + (kt >> 16))];
+              for (int mc = 0; mc < nsc; ++mc) w[mc] += Mk[mc * kEriNKet + jj] * r;
             }
           }
           __syncwarp();  // R buffers are rewritten by the next primitive

@@ -862,6 +862,11 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
         for (int v = 0; v <= r; ++v) tuv[n++] = (sum - r) | ((r - v) << 8) | (v << 16);
     e = cudaMemcpyToSymbol(c_eri_tuv, tuv, sizeof(tuv));
   }
+  if (!e) {
+    double rodd[kEriMaxL + kEriBoysTerms + 1];
+    for (int j = 0; j <= kEriMaxL + kEriBoysTerms; ++j) rodd[j] = 1.0 / (2 * j + 1);
+    e = cudaMemcpyToSymbol(c_eri_rodd, rodd, sizeof(rodd));
+  }
   if (!e) e = cudaFuncSetAttribute(k_eri3c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (!e && !items.empty()) {
     {
