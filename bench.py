@@ -239,14 +239,16 @@ def run_water(dev, reps=2000):
     return res
 
 
-def cpu_reference_build(ds, Cocc, P, kchunk):
-    """One Fock build with the CPU oracle on all host threads (seconds)."""
+def cpu_reference_build(ds, Cocc, P, kchunk, want=False):
+    """One Fock build with the CPU oracle on all host threads: seconds, and
+    with want=True also (J, K)."""
     from oracle.oracle import Oracle
     O = Oracle(ds.layout, ds.B)
     t0 = time.perf_counter()
-    O.df_j(ds.Vinv, 2.0 * P, ds.eps)
-    O.dfmo_k(np.tril(ds.Linv), Cocc, ds.eps, kchunk=kchunk)
-    return time.perf_counter() - t0
+    J = O.df_j(ds.Vinv, 2.0 * P, ds.eps)
+    K = O.dfmo_k(np.tril(ds.Linv), Cocc, ds.eps, kchunk=kchunk)
+    t = time.perf_counter() - t0
+    return (t, J, K) if want else t
 
 
 def run_reference(args):
@@ -701,6 +703,7 @@ def main():
         torch.cuda.synchronize()
         ms64 = f0.elapsed_time(f1) / nst
         Jf, Kf = eng.compute_jk(Ph, Cocc, args.kmethod)
+        Jf, Kf = Jf.copy(), Kf.copy()
         eng.set_jmode("cholesky")
         Jfc, _ = eng.compute_jk(Ph, None, args.kmethod)
         eng.set_jmode("vinv")
@@ -819,7 +822,12 @@ def main():
         out["water"] = run_water(dev)
     if rank == 0 and not args.no_cpu_baseline:
         kc = k_split_plan(nbf, naux, nocc)[1]
-        tcpu = cpu_reference_build(ds, Cocc, P, kc)
+        tcpu, Jo, Ko = cpu_reference_build(ds, Cocc, P, kc, want=True)
+        if fp64 is not None and args.kmethod == "dfmo":
+            # the FP64 device path against the CPU oracle on the same inputs
+            fp64["oracle_max_abs_dJ"] = float(np.abs(Jf - Jo).max())
+            fp64["oracle_max_abs_dK"] = float(np.abs(Kf - Ko).max())
+            fp64["bitwise_vs_oracle"] = bool(np.array_equal(Jf, Jo) and np.array_equal(Kf, Ko))
         out["cpu_baseline"] = {"value": 1.0 / tcpu, "unit": "builds/s", "cores": os.cpu_count(),
                                "kind": "port",
                                "sample": "one full Fock build (DF-J + DF-MO-K), C restatement, "
