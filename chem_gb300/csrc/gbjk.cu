@@ -960,8 +960,8 @@ static gbjk_status run_jk_split(gbjk_ctx* ctx, const double* dP, const double* d
   CK(cudaMemsetAsync(dJ, 0, (size_t)nbf * nbf * sizeof(double), ctx->stream));
   {
     PhaseScope ps(ctx, PH_J_REDUCE);
-    k_reduce_rows<<<cdiv(naux, 128), 128, 0, ctx->stream>>>(ctx->split.d_dpart, nbf, naux,
-                                                            ctx->split.d_dt);
+    k_reduce_rows16<<<cdiv(naux, 32), 512, 0, ctx->stream>>>(ctx->split.d_dpart, nbf, naux,
+                                                             ctx->split.d_dt);
     CKL(PH_J_REDUCE);
   }
   {

@@ -69,6 +69,40 @@ __global__ void k_reduce_rows(const double* __restrict__ part, int nrows, int nc
   g[X] = s;
 }
 
+// g[X] = sum_{mu} part[mu][X] for the mixed path: warp w of a block sums
+// the rows w, w + 16, ... in order (four loads in flight), then the sixteen
+// partial sums are added in warp order.  A fixed order, coalesced row reads,
+// and sixteen times the parallelism of one thread per column.
+__global__ void __launch_bounds__(512)
+    k_reduce_rows16(const double* __restrict__ part, int nrows, int ncols,
+                    double* __restrict__ g) {
+  __shared__ double ps[16][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int X = blockIdx.x * 32 + lane;
+  double s = 0.0;
+  if (X < ncols) {
+    int r = w;
+    for (; r + 48 < nrows; r += 64) {
+      const double a0 = part[(long long)r * ncols + X];
+      const double a1 = part[(long long)(r + 16) * ncols + X];
+      const double a2 = part[(long long)(r + 32) * ncols + X];
+      const double a3 = part[(long long)(r + 48) * ncols + X];
+      s += a0;
+      s += a1;
+      s += a2;
+      s += a3;
+    }
+    for (; r < nrows; r += 16) s += part[(long long)r * ncols + X];
+  }
+  ps[w][lane] = s;
+  __syncthreads();
+  if (w == 0 && X < ncols) {
+    double t = ps[0][lane];
+    for (int i = 1; i < 16; ++i) t += ps[i][lane];
+    g[X] = t;
+  }
+}
+
 // y = M x, M n x n row-major; one warp per row.
 __global__ void k_gemv(const double* __restrict__ M, const double* __restrict__ x, int n,
                        double* __restrict__ y) {
