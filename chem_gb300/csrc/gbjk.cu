@@ -104,6 +104,7 @@ struct gbjk_ctx {
   int wc_nocc = -1;
   int ksplit = 1;
   bool narrow = false;  // half transform and fit on 64 x 16 tiles
+  int ht_tn = 64;        // tile width of the half transform and fit
   bool elem_ht = false, elem_k = false;  // one thread per output (tiny problems)
   double *d_C = nullptr, *d_Cg = nullptr, *d_H = nullptr, *d_H2 = nullptr, *d_Kpart = nullptr,
          *d_K = nullptr;
@@ -296,10 +297,14 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
   const bool elem_ht = (long long)nbf * naux * nocc <= kElemOutputs;
   const bool elem_k = (long long)nbf * nbf * ks <= kElemOutputs;
   const bool narrow = !elem_ht && nocc <= kNarrowN;
+  // occupied widths just above a multiple of 32 (e.g. 81) pad less with
+  // 64 x 32 tiles than with 64 x 64 ones
+  const bool mid = !elem_ht && !narrow && cdiv(nocc, 32) * 32 < cdiv(nocc, 64) * 64;
   ctx->narrow = narrow;
+  ctx->ht_tn = elem_ht || narrow ? 16 : (mid ? 32 : 64);
   ctx->elem_ht = elem_ht;
   ctx->elem_k = elem_k;
-  const int ht_tm = elem_ht ? 16 : 64, ht_tn = elem_ht || narrow ? 16 : 64;
+  const int ht_tm = elem_ht ? 16 : 64, ht_tn = ctx->ht_tn;
   const int k_t = elem_k ? 16 : 64;
 
   std::vector<GemmGroup> groups;
@@ -431,7 +436,7 @@ gbjk_status ensure_j_workspace(gbjk_ctx* ctx) {
 }
 
 gbjk_status launch_gemm(gbjk_ctx* ctx, int tile0, int ntiles, bool transB, double alpha,
-                        int phase, bool narrow = false, bool elem = false) {
+                        int phase, bool narrow = false, bool elem = false, int tn = 64) {
   if (ntiles == 0) return GBJK_OK;
   PhaseScope ps(ctx, phase);
   const GemmGroup* g = ctx->d_groups;
@@ -442,6 +447,8 @@ gbjk_status launch_gemm(gbjk_ctx* ctx, int tile0, int ntiles, bool transB, doubl
     k_gemm_fp64_elem<false><<<ntiles, 256, 0, ctx->stream>>>(g, t, alpha);
   else if (narrow)
     k_gemm_fp64<false, false, 16><<<ntiles, 64, 0, ctx->stream>>>(g, t, alpha);
+  else if (!transB && tn == 32)
+    k_gemm_fp64<false, false, 32><<<ntiles, 128, 0, ctx->stream>>>(g, t, alpha);
   else if (transB)
     k_gemm_fp64<true><<<ntiles, 256, 0, ctx->stream>>>(g, t, alpha);
   else
@@ -529,12 +536,12 @@ gbjk_status run_k(gbjk_ctx* ctx, int kmethod, const double* dC, int nocc, double
     CKL(PH_GATHER);
   }
   if ((s = launch_gemm(ctx, ctx->ht_tile0, ctx->ht_ntiles, false, 1.0, PH_HT, ctx->narrow,
-                       ctx->elem_ht)))
+                       ctx->elem_ht, ctx->ht_tn)))
     return s;
   const bool mo = kmethod == GBJK_K_DFMO || ctx->fitted;
   if (!ctx->fitted &&
       (s = launch_gemm(ctx, mo ? ctx->fit_tile0 : ctx->fitV_tile0, ctx->fit_ntiles, false, 1.0,
-                       PH_FIT, ctx->narrow, ctx->elem_ht)))
+                       PH_FIT, ctx->narrow, ctx->elem_ht, ctx->ht_tn)))
     return s;
   if ((s = launch_gemm(ctx, mo ? ctx->syrk_tile0 : ctx->lmo_tile0,
                        mo ? ctx->syrk_ntiles : ctx->lmo_ntiles, true, 1.0, PH_KGEMM, false,

@@ -307,7 +307,7 @@ __global__ void k_expand_panels(const double* __restrict__ P, const long long* _
       P[panel_off[I] + ((long long)m * naux + X) * KI + k];
 }
 
-// Grouped FP64 GEMM over a tile list; 64 x TN tiles (TN = 64 or 16),
+// Grouped FP64 GEMM over a tile list; 64 x TN tiles (TN = 64, 32 or 16),
 // 16 * TN / 4 threads, 4x4 outputs per thread.  Every output is one in-order
 // fma chain over its k range, whatever the tile shape.
 // TRANSA: A is stored K x M row-major, op(A)(m, k) = A[k * lda + m].
@@ -315,7 +315,7 @@ template <bool TRANSB, bool TRANSA = false, int TN = 64>
 __global__ void __launch_bounds__(TN * 4)
     k_gemm_fp64(const GemmGroup* __restrict__ groups, const GemmTile* __restrict__ tiles,
                 double alpha) {
-  static_assert(TN == 64 || TN == 16, "tile width");
+  static_assert(TN == 64 || TN == 32 || TN == 16, "tile width");
   constexpr int NT = TN * 4;   // threads
   constexpr int CW = TN / 4;   // thread columns
   __shared__ double As[16][65];
