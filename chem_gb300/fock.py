@@ -132,9 +132,9 @@ class _PinnedBuffer:
                                     "data": (self.ptr, False), "version": 3}
 
     def __del__(self):
-        if getattr(self, "ptr", None):
-            lib().gbjk_host_free(self.ptr)
-            self.ptr = None
+        ptr, self.ptr = getattr(self, "ptr", None), None
+        if ptr and _lib is not None:  # at interpreter exit the library may be gone
+            _lib.gbjk_host_free(ptr)
 
 
 def host_array(shape, dtype=np.float64):
