@@ -282,6 +282,10 @@ __device__ void eri_ss_aux(const double* pp, int psz, int npp, const EriShell& c
   }
 }
 
+// SS: the launch holds only s-s shell pairs (lanes over primitive pairs),
+// else only the other pairs; two kernels with half the code each keep the
+// instruction working set of a block small.
+template <bool SS>
 __global__ void __launch_bounds__(32 * kEriWarps, 4)
     k_eri3c(const EriItem* __restrict__ items, const EriShell* __restrict__ ao,
             const EriShell* __restrict__ ax, const double* __restrict__ ao_alpha,
@@ -352,7 +356,7 @@ __global__ void __launch_bounds__(32 * kEriWarps, 4)
       for (int m = 0; m < kEriMaxSph; ++m) acc0[m] = acc1[m] = 0.0;
       const int nck = c.nprim;
       const int qch = kEriRnChunk / nck > 0 ? kEriRnChunk / nck : 1;
-      if (Lb == 0) {
+      if constexpr (SS) {
         // s-s pair: lanes over the bra primitive pairs; every lane ends
         // with the sums, lane 0 stores them as the one cartesian pair
         if (lc == 0)
@@ -368,7 +372,7 @@ __global__ void __launch_bounds__(32 * kEriWarps, 4)
         eri_ket_matrix(lc, ax_alpha[c.prim0], lane, Mk);
         __syncwarp();
       }
-      for (int q0 = 0; q0 < (Lb == 0 ? 0 : npp); q0 += qch) {
+      for (int q0 = 0; q0 < (SS ? 0 : npp); q0 += qch) {
       const int q1 = min(npp, q0 + qch);
       // Boys functions of the chunk's (q, k) combinations, one per lane
       for (int jq = lane; jq < (q1 - q0) * nck; jq += 32) {

@@ -815,8 +815,9 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
   };
   std::vector<EriShell> hao, hax;
   const int npa = shells(ao, hao), npx = shells(aux, hax);
-  std::vector<EriItem> items;
-  size_t bra_max = 0;
+  // work items: s-s shell pairs first (their own kernel), then the rest
+  std::vector<EriItem> items, rest;
+  size_t bra_max[2] = {0, 0};
   for (int p = 0; p < npairs; ++p) {
     const int I = pair_I[p], J = pair_J[p];
     if (I < 0 || J < I || J >= ctx->nblk)
@@ -824,13 +825,19 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
     for (int a = blk_shell_off[I]; a < blk_shell_off[I + 1]; ++a)
       for (int b = blk_shell_off[J]; b < blk_shell_off[J + 1]; ++b) {
         if (I == J && b < a) continue;
-        items.push_back({p, a, b});
         const int la = hao[a].l, lb = hao[b].l;
+        const int ss = la + lb == 0 ? 0 : 1;
+        (ss == 0 ? items : rest).push_back({p, a, b});
         const size_t psz = 6 + 3 * (la + 1) * (lb + 1) * (la + lb + 1);
-        bra_max = std::max(bra_max, (size_t)hao[a].nprim * hao[b].nprim * psz);
+        bra_max[ss] = std::max(bra_max[ss], (size_t)hao[a].nprim * hao[b].nprim * psz);
       }
   }
-  const size_t smem = (bra_max + (size_t)kEriWarps * kEriWarpDoubles) * sizeof(double);
+  const size_t n_ss = items.size();
+  items.insert(items.end(), rest.begin(), rest.end());
+  size_t smem_k[2];
+  for (int k = 0; k < 2; ++k)
+    smem_k[k] = (bra_max[k] + (size_t)kEriWarps * kEriWarpDoubles) * sizeof(double);
+  const size_t smem = std::max(smem_k[0], smem_k[1]);
   if (smem > 200 * 1024)
     return fail(ctx, GBJK_INVALID_ARG, "gbjk_upload_b_eri3c: contraction too long for the kernel");
   gbjk_status s;
@@ -874,21 +881,30 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
     for (int j = 0; j <= kEriMaxL + kEriBoysTerms; ++j) rodd[j] = 1.0 / (2 * j + 1);
     e = cudaMemcpyToSymbol(c_eri_rodd, rodd, sizeof(rodd));
   }
-  if (!e) e = cudaFuncSetAttribute(k_eri3c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (!e)
+    e = cudaFuncSetAttribute(k_eri3c<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_k[0]);
+  if (!e)
+    e = cudaFuncSetAttribute(k_eri3c<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)smem_k[1]);
   if (!e && !items.empty()) {
     {
       PhaseScope ps(ctx, PH_GATHER);
-      for (size_t i0 = 0; i0 < items.size(); i0 += (1u << 30)) {
-        const int n = (int)std::min<size_t>(1u << 30, items.size() - i0);
-        k_eri3c<<<n, 32 * kEriWarps, smem, ctx->stream>>>(
-            (const EriItem*)d_items + i0, (const EriShell*)d_ao, (const EriShell*)d_ax,
-            (const double*)d_aoa, (const double*)d_aoc, (const double*)d_axa,
-            (const double*)d_axc, (const int*)d_pI, (const int*)d_pJ,
-            (const unsigned char*)d_keep, nablk, (const int*)d_aoff, ctx->d_boff,
-            ctx->d_panel_off, ctx->d_panelK, (const int*)d_cij, (const int*)d_cji, ctx->naux,
-            ctx->d_B);
-        ctx->launches++;
-      }
+      // [0, n_ss): s-s pairs, [n_ss, end): the others; grid slices of 2^30
+      const size_t seg[3] = {0, n_ss, items.size()};
+      for (int k = 0; k < 2; ++k)
+        for (size_t i0 = seg[k]; i0 < seg[k + 1]; i0 += (1u << 30)) {
+          const int n = (int)std::min<size_t>(1u << 30, seg[k + 1] - i0);
+          auto kern = k == 0 ? k_eri3c<true> : k_eri3c<false>;
+          kern<<<n, 32 * kEriWarps, smem_k[k], ctx->stream>>>(
+              (const EriItem*)d_items + i0, (const EriShell*)d_ao, (const EriShell*)d_ax,
+              (const double*)d_aoa, (const double*)d_aoc, (const double*)d_axa,
+              (const double*)d_axc, (const int*)d_pI, (const int*)d_pJ,
+              (const unsigned char*)d_keep, nablk, (const int*)d_aoff, ctx->d_boff,
+              ctx->d_panel_off, ctx->d_panelK, (const int*)d_cij, (const int*)d_cji, ctx->naux,
+              ctx->d_B);
+          ctx->launches++;
+        }
     }
     e = cudaGetLastError();
     if (!e) e = cudaStreamSynchronize(ctx->stream);
