@@ -662,15 +662,40 @@ def main():
         # profiles/k_split_gemm_c14h30.md (2.045 GB for 1.6618e8 tensor
         # elements), scaled by the tensor elements of this workload
         traffic = 2.045e9 / 1.6618e8 * nnz if name == "split_gemm_ht" else None
+        tensor = {"achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
+                  "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)",
+                  "algorithmic_flops_per_launch": f,
+                  "flops_definition": "15 BF16 digit-pair products x 2*M*N*K of the unpadded "
+                                      "FP64 product (M*N*K = nocc*nnz(B) for the half "
+                                      "transform)"}
         roof = {"kernel": "k_split_gemm (" + name + ")", "bound": "tensor", "achieved": ach,
                 "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16, "traffic": traffic,
                 "traffic_source": "ncu capture on C14H30 scaled by tensor elements",
-                "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)",
-                "algorithmic_flops_per_launch": f,
-                "flops_definition": "15 BF16 digit-pair products x 2*M*N*K of the unpadded "
-                                    "FP64 product (M*N*K = nocc*nnz(B) for the half transform)",
+                "peak_source": tensor["peak_source"], "algorithmic_flops_per_launch": f,
+                "flops_definition": tensor["flops_definition"],
                 "fp64_equivalent_tflops": flops64[name] / (per_launch_ms * 1e-3) / 1e12,
                 "ms_per_launch": per_launch_ms}
+        if name == "split_gemm_ht":
+            # algorithmic bytes of one launch: the digit slices of L^-1 B
+            # (five BF16 digits per tensor element, read once), the FP64
+            # H written (nocc columns) with the density-row partials, and
+            # the digit slices of C and of the density rows per panel
+            lay = ds.layout
+            cdig = sum(10.0 * int(k) * (nocc + int(b)) for k, b in zip(lay.panel_K, lay.bsizes))
+            byts = 10.0 * nnz + 8.0 * nbf * naux * (nocc + 1) + cdig
+            ai, ridge = f / byts, bf16 * 1e12 / (hbm * 1e9)
+            if ai < ridge:  # below the ridge point: HBM bounds the launch
+                achb = byts / (per_launch_ms * 1e-3) / 1e9
+                roof.update({"bound": "hbm", "achieved": achb, "peak": hbm, "unit": "GB/s",
+                             "frac": achb / hbm, "peak_source": f"{src} (MEASURED_PEAKS.json "
+                                                               "hbm_gbs)",
+                             "algorithmic_bytes_per_launch": byts,
+                             "bytes_definition": "10 B per tensor element (digit slices of "
+                                                 "L^-1 B) + 8 B per H element and density "
+                                                 "partial written + digit slices of C and "
+                                                 "the density rows",
+                             "arithmetic_intensity_flop_per_byte": ai,
+                             "ridge_flop_per_byte": ridge, "tensor_pipe": tensor})
     elif name in flops64:
         fp64_peak = 1250.0  # GB300 nominal FP64 (GFLOP/s), not in MEASURED_PEAKS.json
         ach = flops64[name] / (per_launch_ms * 1e-3) / 1e12
