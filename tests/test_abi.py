@@ -51,3 +51,21 @@ def test_product_has_no_oracle_import():
             if f.endswith(".py"):
                 src = open(os.path.join(dirpath, f)).read()
                 assert "oracle" not in re.sub(r"#.*|\"\"\"[\s\S]*?\"\"\"", "", src), f
+
+
+def test_k_split_plan_covers_the_sum_in_aligned_chunks():
+    # gbjk_k_split_plan needs no GPU: the chunks are multiples of 16, cover
+    # the naux*nocc terms exactly once, hold at least 64 terms when split,
+    # and split further for small exchange matrices (fewer output tiles)
+    from chem_gb300.fock import k_split_plan
+    for nbf, naux, nocc in [(24, 116, 5), (106, 510, 17), (490, 2366, 81), (970, 4686, 161),
+                            (4000, 12000, 600), (7, 3, 1)]:
+        ks, kc = k_split_plan(nbf, naux, nocc)
+        kdim = naux * nocc
+        assert ks >= 1 and kc % 16 == 0
+        assert (ks - 1) * kc < kdim <= ks * kc
+        assert ks == 1 or kc >= 64
+    # water: one 64 x 64 output tile, 580 terms, still spread over parts
+    assert k_split_plan(24, 116, 5)[0] > 1
+    with pytest.raises(RuntimeError):
+        k_split_plan(0, 116, 5)
