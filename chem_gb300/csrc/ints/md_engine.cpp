@@ -15,22 +15,9 @@ namespace gbints {
 // so no cancellation).  Large T: F_0 = sqrt(pi/T) erf(sqrt T) / 2 and the
 // upward recursion F_{m+1} = ((2m+1) F_m - exp(-T)) / (2T), which is stable
 // there because exp(-T) is negligible against (2m+1) F_m.
-// The divisions by odd integers are products with tabulated reciprocals.
-namespace {
-constexpr int kBoysTerms = 400;
-struct OddReciprocals {
-  double r[kMaxLTot + kBoysTerms + 1];
-  OddReciprocals() {
-    for (int j = 0; j <= kMaxLTot + kBoysTerms; ++j) r[j] = 1.0 / (2 * j + 1);
-  }
-};
-const OddReciprocals kOdd;
-}  // namespace
-
 void boys(int nmax, double T, double* F) {
-  const double* rodd = kOdd.r;
   if (T < 1e-15) {
-    for (int m = 0; m <= nmax; ++m) F[m] = rodd[m];
+    for (int m = 0; m <= nmax; ++m) F[m] = 1.0 / (2 * m + 1);
     return;
   }
   const double eT = std::exp(-T);
@@ -40,16 +27,18 @@ void boys(int nmax, double T, double* F) {
     for (int m = 0; m < nmax; ++m) F[m + 1] = ((2 * m + 1) * F[m] - eT) * inv2T;
     return;
   }
-  double term = rodd[nmax];
+  double denom = 2 * nmax + 1;
+  double term = 1.0 / denom;
   double sum = term;
   const double twoT = 2.0 * T;
-  for (int k = 1; k < kBoysTerms; ++k) {
-    term *= twoT * rodd[nmax + k];
+  for (int k = 1; k < 400; ++k) {
+    denom += 2.0;
+    term *= twoT / denom;
     sum += term;
     if (term < 1e-17 * sum) break;
   }
   F[nmax] = eT * sum;
-  for (int m = nmax - 1; m >= 0; --m) F[m] = (twoT * F[m + 1] + eT) * rodd[m];
+  for (int m = nmax - 1; m >= 0; --m) F[m] = (twoT * F[m + 1] + eT) / (2 * m + 1);
 }
 
 void cart_exponents(int l, int c, int* ex) {
