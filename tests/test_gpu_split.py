@@ -44,7 +44,9 @@ def test_split_k_vs_oracle(sysname, request):
           f"{np.abs(J - Jr).max():.3e} (V^-1 route)  max|J| = {np.abs(Jr).max():.3f}")
     assert dK <= 1e-9
     assert dJ <= 1e-9
-    assert np.abs(J - Jr).max() <= 1e-8
+    # against the V^-1 route: no farther than that route's own rounding
+    # noise (|Jc - Jr|, ~1e-8 for decane) plus the split error
+    assert np.abs(J - Jr).max() <= np.abs(Jc - Jr).max() + 1e-9
     # and against the device FP64 path on the Cholesky route
     eng.set_precision("fp64")
     eng.set_jmode("cholesky")
