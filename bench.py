@@ -32,7 +32,9 @@ METRIC = "Fock builds/s (DF-J + DF-K)"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 Fock builds, about half a second "
+                         "of device time; 10 for the other workloads and the reference arm)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="split", choices=["fp64", "split"])
@@ -59,7 +61,10 @@ def parse():
     ap.add_argument("--slots", type=int, default=4)
     ap.add_argument("--alkane-max", type=int, default=40)
     ap.add_argument("--water-max", type=int, default=32)
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 200 if args.workload == "fock" and args.impl == "ours" else 10
+    return args
 
 
 def setup(nC):
@@ -112,7 +117,7 @@ class ClockSampler:
                     self.samples.append([v.strip() for v in out.split(",")])
             except Exception:
                 pass
-            self._stop.wait(0.2)
+            self._stop.wait(0.1)
 
     def __enter__(self):
         self._t = threading.Thread(target=self._run, daemon=True)
