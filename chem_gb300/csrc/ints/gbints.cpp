@@ -251,9 +251,35 @@ void shell_pair_2c(const Shell& a, const Shell& c, std::vector<double>& out) {
 // 3-center (X|ab) for one AO shell pair (a, b) against a list of auxiliary
 // shells.  Output in cartesian a,b and spherical X:
 //   acc[ca][cb][xoff(k) + mx]   for aux shell k of the list.
+// Ket side of an auxiliary shell, per primitive and cartesian component:
+// its single-centre Hermite terms with the sign (-1)^(t+u+v) of the Coulomb
+// kernel folded into the coefficient (a product with +-1, so exact).  It
+// depends on the auxiliary shell only, so it is built once per tensor rather
+// than once per bra primitive pair.
+struct KetTable {
+  std::vector<std::vector<std::vector<HermTerm>>> terms;  // [prim][cc]
+};
+
+KetTable make_ket_table(const Shell& c) {
+  KetTable t;
+  t.terms.resize(c.alpha.size());
+  PrimPair ket;
+  for (size_t ic = 0; ic < c.alpha.size(); ++ic) {
+    make_single(c, (int)ic, ket);
+    t.terms[ic].resize(c.ncart());
+    for (int cc = 0; cc < c.ncart(); ++cc) {
+      herm_terms(ket, c.l, cc, 0, 0, t.terms[ic][cc]);
+      for (auto& h : t.terms[ic][cc])
+        if ((h.t + h.u + h.v) & 1) h.c = -h.c;
+    }
+  }
+  return t;
+}
+
 struct Aux3c {
   const Shell* sh;
-  int xoff;  // offset of the shell's functions in the output row
+  int xoff;                    // offset of the shell's functions in the output row
+  const KetTable* ket = nullptr;  // ket terms of the shell
 };
 
 void pair_vs_aux(const Shell& a, const Shell& b, const std::vector<Aux3c>& aux, int nxtot,
@@ -261,8 +287,7 @@ void pair_vs_aux(const Shell& a, const Shell& b, const std::vector<Aux3c>& aux, 
   const int nca = a.ncart(), ncb = b.ncart();
   acc.assign((size_t)nca * ncb * nxtot, 0.0);
   static thread_local HermR R;
-  std::vector<HermTerm> tb, tk;
-  PrimPair bra, ket;
+  PrimPair bra;
   const int Lb = a.l + b.l;
   const int S = Lb + 1;
   std::vector<double> W;
@@ -280,22 +305,17 @@ void pair_vs_aux(const Shell& a, const Shell& b, const std::vector<Aux3c>& aux, 
         // Wsph[tuv][mc]
         W.assign((size_t)S * S * S * nsc, 0.0);
         for (size_t ic = 0; ic < c.alpha.size(); ++ic) {
-          make_single(c, ic, ket);
-          const double p = bra.p, q = ket.p;
+          const double p = bra.p, q = c.alpha[ic];
           const double alpha = p * q / (p + q);
-          const double pref = kTwoPi52 / (p * q * std::sqrt(p + q)) * bra.coef * ket.coef;
-          hermite_r(Lb + lc, alpha, bra.P[0] - ket.P[0], bra.P[1] - ket.P[1],
-                    bra.P[2] - ket.P[2], R);
+          const double pref = kTwoPi52 / (p * q * std::sqrt(p + q)) * bra.coef * c.coef[ic];
+          hermite_r(Lb + lc, alpha, bra.P[0] - c.A[0], bra.P[1] - c.A[1], bra.P[2] - c.A[2], R);
           for (int cc = 0; cc < ncc; ++cc) {
-            herm_terms(ket, lc, cc, 0, 0, tk);
+            const std::vector<HermTerm>& tk = ax.ket->terms[ic][cc];
             for (int t = 0; t <= Lb; ++t)
               for (int u = 0; u <= Lb - t; ++u)
                 for (int v = 0; v <= Lb - t - u; ++v) {
                   double s = 0.0;
-                  for (const auto& h : tk) {
-                    const double sg = ((h.t + h.u + h.v) & 1) ? -1.0 : 1.0;
-                    s += sg * h.c * R.r[t + h.t][u + h.u][v + h.v];
-                  }
+                  for (const auto& h : tk) s += h.c * R.r[t + h.t][u + h.u][v + h.v];
                   s *= pref;
                   double* w = W.data() + (((size_t)t * S + u) * S + v) * nsc;
                   for (int mc = 0; mc < nsc; ++mc) w[mc] += sc[mc * ncc + cc] * s;
@@ -591,6 +611,8 @@ int gbints_eri3c_panels(const gbints_basis* ao, const gbints_basis* aux, int nbl
         items.push_back({p, a, b});
       }
   }
+  std::vector<KetTable> kets(AX.shells.size());
+  for (size_t s = 0; s < AX.shells.size(); ++s) kets[s] = make_ket_table(AX.shells[s]);
 #pragma omp parallel for schedule(dynamic, 1) num_threads(threads_or_default(nthreads))
   for (long k = 0; k < (long)items.size(); ++k) {
     const Item it = items[k];
@@ -602,7 +624,7 @@ int gbints_eri3c_panels(const gbints_basis* ao, const gbints_basis* aux, int nbl
     for (int A = 0; A < nablk; ++A) {
       if (!keep[(size_t)it.p * nablk + A]) continue;
       for (int s = ablk_shell_off[A]; s < ablk_shell_off[A + 1]; ++s) {
-        list.push_back({&AX.shells[s], nx});
+        list.push_back({&AX.shells[s], nx, &kets[s]});
         nx += AX.shells[s].nsph();
       }
     }
