@@ -15,7 +15,9 @@ namespace gbints {
 // so no cancellation).  Large T: F_0 = sqrt(pi/T) erf(sqrt T) / 2 and the
 // upward recursion F_{m+1} = ((2m+1) F_m - exp(-T)) / (2T), which is stable
 // there because exp(-T) is negligible against (2m+1) F_m.
-void boys(int nmax, double T, double* F) {
+namespace {
+// Series form (also fills the interpolation grid below).
+void boys_series(int nmax, double T, double* F) {
   if (T < 1e-15) {
     for (int m = 0; m <= nmax; ++m) F[m] = 1.0 / (2 * m + 1);
     return;
@@ -39,6 +41,40 @@ void boys(int nmax, double T, double* F) {
   }
   F[nmax] = eT * sum;
   for (int m = nmax - 1; m >= 0; --m) F[m] = (twoT * F[m + 1] + eT) / (2 * m + 1);
+}
+
+// F_m on the grid T_i = i h, m < kGridM, computed once by the series.  Since
+// dF_m/dT = -F_{m+1}, the Taylor expansion about the nearest grid point,
+//   F_m(T) = sum_{k<7} F_{m+k}(T_i) (T_i - T)^k / k!,  |T - T_i| <= h / 2,
+// has a remainder below F_m (h/2)^7 / 7! = 1.2e-15 F_m for h = 1/20.
+constexpr double kGridH = 0.05;
+constexpr int kTaylor = 7;
+constexpr int kGridM = kMaxLTot + kTaylor;
+struct BoysGrid {
+  int n;
+  std::vector<double> f;  // [i][m]
+  BoysGrid() {
+    n = (int)((33.0 + kMaxLTot) / kGridH) + 2;
+    f.resize((size_t)n * kGridM);
+    for (int i = 0; i < n; ++i) boys_series(kGridM - 1, i * kGridH, &f[(size_t)i * kGridM]);
+  }
+};
+const BoysGrid kGrid;
+}  // namespace
+
+void boys(int nmax, double T, double* F) {
+  if (T > 33.0 + nmax) {
+    boys_series(nmax, T, F);  // erf and upward recursion
+    return;
+  }
+  const int i = (int)(T * (1.0 / kGridH) + 0.5);
+  const double x = i * kGridH - T;
+  const double* g = kGrid.f.data() + (size_t)i * kGridM;
+  for (int m = 0; m <= nmax; ++m) {
+    double s = g[m + kTaylor - 1];
+    for (int k = kTaylor - 1; k >= 1; --k) s = g[m + k - 1] + (x / k) * s;
+    F[m] = s;
+  }
 }
 
 void cart_exponents(int l, int c, int* ex) {
