@@ -784,6 +784,33 @@ def main():
                 "max_abs_dK_fp64_dfao_vs_fp64_dfmo": float(np.abs(res["fp64"][1] - Kmo64).max()),
                 "dE_K_split_vs_fp64_Eh": float(np.sum(P * (res["split"][1] - res["fp64"][1])))}
 
+    # non-symmetric DF-LMO K (the ADC caller's left/right coefficients):
+    # split and FP64 call times through the host-buffer entry point; a
+    # failure here is recorded and does not stop the bench line
+    asym = None
+    if args.precision == "split" and not args.no_dfao:
+        try:
+            rng = np.random.default_rng(9)
+            U = Cocc + 0.1 * rng.standard_normal(Cocc.shape)
+            Vt = np.ascontiguousarray((Cocc + 0.1 * rng.standard_normal(Cocc.shape)).T)
+            res, Ka = {}, {}
+            for prec, nst in (("split", 10), ("fp64", 3)):
+                eng.set_precision(prec)
+                Ka[prec] = eng.compute_k_lmo_asym(U, Vt)  # plans and warm-up
+                t0 = time.perf_counter()
+                for _ in range(nst):
+                    eng.compute_k_lmo_asym(U, Vt)
+                res[prec + "_ms"] = (time.perf_counter() - t0) / nst * 1e3
+            eng.set_precision(args.precision)
+            asym = dict(res, speedup=res["fp64_ms"] / res["split_ms"],
+                        max_abs_dK_split_vs_fp64=float(np.abs(Ka["split"] - Ka["fp64"]).max()),
+                        max_abs_K=float(np.abs(Ka["fp64"]).max()),
+                        timing="host wall clock per gbjk_compute_k_lmo_asym call "
+                               "(host buffers in and out)")
+        except Exception as e:  # recorded in the line, the bench goes on
+            eng.set_precision(args.precision)
+            asym = {"error": str(e)[:300]}
+
     # full DF-HF SCF (the config's SCF comparison): FP64 on the reference
     # route, FP64 on the Cholesky route, mixed precision switching to FP64
     # (Cholesky route) once the DIIS error is below 1e-5
@@ -843,6 +870,7 @@ def main():
         "roofline": roof,
         "fp64_gpu": fp64,
         "dfao_k": dfao,
+        "adc_asym_k": asym,
         "scf": scf,
         "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items() if v[1]},
         "clocks": clk.summary(),
