@@ -94,7 +94,8 @@ def test_boys_against_mpmath():
     # between unnormalised-by-hand single primitives has the closed form
     # (a|b) = 2 pi^{5/2} / (a b sqrt(a+b)) F_0(a b/(a+b) R^2) N_a N_b
     a, b = 0.8, 1.7
-    for R in [0.0, 0.3, 2.0, 7.5, 15.0]:
+    # T = 0.544 R^2: 0, 0.05, 2.2, 10.1 (Taylor grid), 20.3, 30.6, 122 (asymptotic)
+    for R in [0.0, 0.3, 2.0, 4.3, 6.11, 7.5, 15.0]:
         mol = Molecule(["H", "H"], np.array([[0, 0, 0], [0, 0, R + 1e-300]]), "sto-3g",
                        "cc-pvdz-jkfit")
         mol.dfbasis.shells = mol.dfbasis.shells[:1]
