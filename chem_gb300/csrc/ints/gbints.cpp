@@ -258,19 +258,24 @@ void shell_pair_2c(const Shell& a, const Shell& c, std::vector<double>& out) {
 // than once per bra primitive pair.
 struct KetTable {
   std::vector<std::vector<std::vector<HermTerm>>> terms;  // [prim][cc]
+  std::vector<std::vector<std::vector<int>>> roff;        // flat R offsets of the terms
 };
 
 KetTable make_ket_table(const Shell& c) {
   KetTable t;
   t.terms.resize(c.alpha.size());
+  t.roff.resize(c.alpha.size());
   PrimPair ket;
   for (size_t ic = 0; ic < c.alpha.size(); ++ic) {
     make_single(c, (int)ic, ket);
     t.terms[ic].resize(c.ncart());
+    t.roff[ic].resize(c.ncart());
     for (int cc = 0; cc < c.ncart(); ++cc) {
       herm_terms(ket, c.l, cc, 0, 0, t.terms[ic][cc]);
-      for (auto& h : t.terms[ic][cc])
+      for (auto& h : t.terms[ic][cc]) {
         if ((h.t + h.u + h.v) & 1) h.c = -h.c;
+        t.roff[ic][cc].push_back((h.t * HermR::S + h.u) * HermR::S + h.v);
+      }
     }
   }
   return t;
@@ -311,11 +316,16 @@ void pair_vs_aux(const Shell& a, const Shell& b, const std::vector<Aux3c>& aux, 
           hermite_r(Lb + lc, alpha, bra.P[0] - c.A[0], bra.P[1] - c.A[1], bra.P[2] - c.A[2], R);
           for (int cc = 0; cc < ncc; ++cc) {
             const std::vector<HermTerm>& tk = ax.ket->terms[ic][cc];
+            const HermTerm* tb = tk.data();
+            const int nt = (int)tk.size();
+            const int* toff = ax.ket->roff[ic][cc].data();
+            const double* R0 = &R.r[0][0][0];
             for (int t = 0; t <= Lb; ++t)
               for (int u = 0; u <= Lb - t; ++u)
                 for (int v = 0; v <= Lb - t - u; ++v) {
                   double s = 0.0;
-                  for (const auto& h : tk) s += h.c * R.r[t + h.t][u + h.u][v + h.v];
+                  const double* Rb = R0 + (t * HermR::S + u) * HermR::S + v;
+                  for (int q = 0; q < nt; ++q) s += tb[q].c * Rb[toff[q]];
                   s *= pref;
                   double* w = W.data() + (((size_t)t * S + u) * S + v) * nsc;
                   for (int mc = 0; mc < nsc; ++mc) w[mc] += sc[mc * ncc + cc] * s;
