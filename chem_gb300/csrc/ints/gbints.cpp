@@ -290,7 +290,11 @@ struct Aux3c {
 void pair_vs_aux(const Shell& a, const Shell& b, const std::vector<Aux3c>& aux, int nxtot,
                  std::vector<double>& acc) {
   const int nca = a.ncart(), ncb = b.ncart();
-  acc.assign((size_t)nca * ncb * nxtot, 0.0);
+  // the auxiliary index stays cartesian through the primitive loops and is
+  // transformed to spherical once at the end (not once per primitive pair)
+  int nxc = 0;
+  for (const auto& ax : aux) nxc += ax.sh->ncart();
+  std::vector<double> accc((size_t)nca * ncb * nxc, 0.0);
   static thread_local HermR R;
   PrimPair bra;
   const int Lb = a.l + b.l;
@@ -303,44 +307,61 @@ void pair_vs_aux(const Shell& a, const Shell& b, const std::vector<Aux3c>& aux, 
       if (std::fabs(bra.coef * bra.E[0].e[0][0][0]) < kPrimCut) continue;
       for (int ca = 0; ca < nca; ++ca)
         for (int cb = 0; cb < ncb; ++cb) herm_terms(bra, a.l, ca, b.l, cb, braterms[ca * ncb + cb]);
+      int xc = 0;
       for (const auto& ax : aux) {
         const Shell& c = *ax.sh;
-        const int lc = c.l, ncc = c.ncart(), nsc = c.nsph();
-        const auto& sc = sph_coeffs(lc);
-        // Wsph[tuv][mc]
-        W.assign((size_t)S * S * S * nsc, 0.0);
+        const int lc = c.l, ncc = c.ncart();
+        // W[tuv][cc], cartesian auxiliary components
+        W.assign((size_t)S * S * S * ncc, 0.0);
         for (size_t ic = 0; ic < c.alpha.size(); ++ic) {
           const double p = bra.p, q = c.alpha[ic];
           const double alpha = p * q / (p + q);
           const double pref = kTwoPi52 / (p * q * std::sqrt(p + q)) * bra.coef * c.coef[ic];
           hermite_r(Lb + lc, alpha, bra.P[0] - c.A[0], bra.P[1] - c.A[1], bra.P[2] - c.A[2], R);
+          const double* R0 = &R.r[0][0][0];
           for (int cc = 0; cc < ncc; ++cc) {
             const std::vector<HermTerm>& tk = ax.ket->terms[ic][cc];
             const HermTerm* tb = tk.data();
             const int nt = (int)tk.size();
             const int* toff = ax.ket->roff[ic][cc].data();
-            const double* R0 = &R.r[0][0][0];
             for (int t = 0; t <= Lb; ++t)
               for (int u = 0; u <= Lb - t; ++u)
                 for (int v = 0; v <= Lb - t - u; ++v) {
                   double s = 0.0;
                   const double* Rb = R0 + (t * HermR::S + u) * HermR::S + v;
                   for (int q = 0; q < nt; ++q) s += tb[q].c * Rb[toff[q]];
-                  s *= pref;
-                  double* w = W.data() + (((size_t)t * S + u) * S + v) * nsc;
-                  for (int mc = 0; mc < nsc; ++mc) w[mc] += sc[mc * ncc + cc] * s;
+                  W[(((size_t)t * S + u) * S + v) * ncc + cc] += pref * s;
                 }
           }
         }
         for (int cab = 0; cab < nca * ncb; ++cab) {
-          double* dst = acc.data() + (size_t)cab * nxtot + ax.xoff;
+          double* dst = accc.data() + (size_t)cab * nxc + xc;
           for (const auto& h : braterms[cab]) {
-            const double* w = W.data() + (((size_t)h.t * S + h.u) * S + h.v) * nsc;
-            for (int mc = 0; mc < nsc; ++mc) dst[mc] += h.c * w[mc];
+            const double* w = W.data() + (((size_t)h.t * S + h.u) * S + h.v) * ncc;
+            for (int cc = 0; cc < ncc; ++cc) dst[cc] += h.c * w[cc];
           }
         }
+        xc += ncc;
       }
     }
+  // spherical auxiliary components: acc[cab][xoff + mc]
+  acc.assign((size_t)nca * ncb * nxtot, 0.0);
+  int xc = 0;
+  for (const auto& ax : aux) {
+    const Shell& c = *ax.sh;
+    const int ncc = c.ncart(), nsc = c.nsph();
+    const auto& sc = sph_coeffs(c.l);
+    for (int cab = 0; cab < nca * ncb; ++cab) {
+      const double* src = accc.data() + (size_t)cab * nxc + xc;
+      double* dst = acc.data() + (size_t)cab * nxtot + ax.xoff;
+      for (int mc = 0; mc < nsc; ++mc) {
+        double v = 0.0;
+        for (int cc = 0; cc < ncc; ++cc) v += sc[mc * ncc + cc] * src[cc];
+        dst[mc] = v;
+      }
+    }
+    xc += ncc;
+  }
 }
 
 // One-electron integrals over a shell pair: which = 0 overlap, 1 kinetic,
