@@ -34,12 +34,17 @@ def test_ragged_panels_and_single_orbital(h2_far):
         kc = k_split_plan(ds.nbf, ds.naux, nocc)[1]
         assert np.array_equal(J, O.df_j(ds.Vinv, 2 * P, 1e-10))
         assert np.array_equal(K, O.dfmo_k(np.tril(ds.Linv), C, 1e-10, kchunk=kc))
+        e64.set_jmode("cholesky")
+        Jc, _ = e64.compute_jk(2 * P, None)
         e64.close()
         es = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=1e-10, precision="split")
         Js, Ks = es.compute_jk(2 * P, C)
         es.close()
         assert np.abs(Ks - K).max() <= 1e-10
-        assert np.abs(Js - J).max() <= 1e-8
+        # the mixed J follows the Cholesky route of the metric; against the
+        # V^-1 route it may differ by that route's own rounding as well
+        assert np.abs(Js - Jc).max() <= 1e-9
+        assert np.abs(Js - J).max() <= np.abs(Jc - J).max() + 1e-9
         # J of a screened block pair is an exact zero in both paths (K is
         # not: delocalised orbitals couple the two molecules)
         bo = ds.layout.boff
