@@ -663,9 +663,10 @@ def main():
     if name.startswith("split_gemm"):
         f = pairs * flops64[name]
         ach = f / (per_launch_ms * 1e-3) / 1e12
-        # DRAM bytes per launch of the half transform from the ncu capture in
-        # profiles/k_split_gemm_c14h30.md (2.045 GB for 1.6618e8 tensor
-        # elements), scaled by the tensor elements of this workload
+        # DRAM bytes per launch of the half transform, read+write, from one
+        # ncu capture of the same kernel on n-C14H30 / cc-pVDZ-jkfit
+        # (2.045 GB for 1.6618e8 tensor elements), scaled by the tensor
+        # elements of this workload
         traffic = 2.045e9 / 1.6618e8 * nnz if name == "split_gemm_ht" else None
         tensor = {"achieved": ach, "peak": bf16, "unit": "TFLOP/s", "frac": ach / bf16,
                   "peak_source": f"{src} (MEASURED_PEAKS.json bf16_tflops, burst)",

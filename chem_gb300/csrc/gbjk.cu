@@ -1408,6 +1408,10 @@ namespace {
 
 constexpr size_t kNoallocScratchBytes = 16u << 20;  // 16 MiB
 constexpr int kNoallocMaxDevices = 64;
+// Atom blocks per call: the block sizes and panel widths travel inside the
+// kernel arguments (8 KB), so a call copies nothing from host memory and
+// issues only launches and memsets.
+constexpr int kNoallocMaxBlocks = 1024;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
 
@@ -1417,10 +1421,21 @@ std::mutex g_noalloc_mu;
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+struct NoallocLayout {
+  int nblk;
+  int bsize[kNoallocMaxBlocks];
+  int panelK[kNoallocMaxBlocks];
+};
+
 // Prefix sums of the layout inside the scratch array (one block).
-__global__ void k_noalloc_layout(int nbf, int naux, int nblk, const int* __restrict__ bsize,
-                                 const int* __restrict__ panelK, int* boff, int* cmoff,
-                                 long long* panel_off, long long* pg_off, int* blk_of) {
+__global__ void k_noalloc_layout(int nbf, int naux, const NoallocLayout lay, int* bsize,
+                                 int* panelK, int* boff, int* cmoff, long long* panel_off,
+                                 long long* pg_off, int* blk_of) {
+  const int nblk = lay.nblk;
+  for (int I = threadIdx.x; I < nblk; I += blockDim.x) {
+    bsize[I] = lay.bsize[I];
+    panelK[I] = lay.panelK[I];
+  }
   if (threadIdx.x == 0) {
     int b = 0, c = 0;
     long long po = 0, pg = 0;
@@ -1429,17 +1444,17 @@ __global__ void k_noalloc_layout(int nbf, int naux, int nblk, const int* __restr
       cmoff[I] = c;
       panel_off[I] = po;
       pg_off[I] = pg;
-      b += bsize[I];
-      c += panelK[I];
-      po += (long long)bsize[I] * naux * panelK[I];
-      pg += (long long)bsize[I] * panelK[I];
+      b += lay.bsize[I];
+      c += lay.panelK[I];
+      po += (long long)lay.bsize[I] * naux * lay.panelK[I];
+      pg += (long long)lay.bsize[I] * lay.panelK[I];
     }
     boff[nblk] = b;
     cmoff[nblk] = c;
   }
   __syncthreads();
   for (int I = 0; I < nblk; ++I)
-    for (int m = threadIdx.x; m < bsize[I]; m += blockDim.x) blk_of[boff[I] + m] = I;
+    for (int m = threadIdx.x; m < lay.bsize[I]; m += blockDim.x) blk_of[boff[I] + m] = I;
 }
 
 }  // namespace
@@ -1459,6 +1474,11 @@ extern "C" gbjk_status gbjk_compute_j_noalloc(const gbjk_desc* d, const int* d_c
   const int nbf = d->nbf, naux = d->naux, nblk = d->nblk;
   if (nbf <= 0 || naux <= 0 || nblk <= 0)
     return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: sizes must be positive");
+  if (nblk > kNoallocMaxBlocks)
+    return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: more than " +
+                                     std::to_string(kNoallocMaxBlocks) + " atom blocks");
+  if (nbf > 65535)  // grid.y of the gather and column-sum launches
+    return err(GBJK_INVALID_ARG, "gbjk_compute_j_noalloc: nbf > 65535 not supported");
   long long bsum = 0, pg_total = 0;
   int maxK = 0;
   for (int I = 0; I < nblk; ++I) {
@@ -1522,13 +1542,13 @@ extern "C" gbjk_status gbjk_compute_j_noalloc(const gbjk_desc* d, const int* d_c
                             : err(GBJK_CUDA_ERROR, std::string(what) + ": " + cudaGetErrorString(e));
   };
   gbjk_status s;
-  if ((s = ck(cudaMemcpyAsync(bsize, d->blk_size, sizeof(int) * nblk, cudaMemcpyHostToDevice, st),
-              "copy block sizes")))
-    return s;
-  if ((s = ck(cudaMemcpyAsync(panelK, d->panel_K, sizeof(int) * nblk, cudaMemcpyHostToDevice, st),
-              "copy panel widths")))
-    return s;
-  k_noalloc_layout<<<1, 256, 0, st>>>(nbf, naux, nblk, bsize, panelK, boff, cmoff, poff, pgoff,
+  NoallocLayout lay;
+  lay.nblk = nblk;
+  for (int I = 0; I < nblk; ++I) {
+    lay.bsize[I] = d->blk_size[I];
+    lay.panelK[I] = d->panel_K[I];
+  }
+  k_noalloc_layout<<<1, 256, 0, st>>>(nbf, naux, lay, bsize, panelK, boff, cmoff, poff, pgoff,
                                       blk_of);
   if ((s = ck(cudaGetLastError(), "layout kernel"))) return s;
   if ((s = ck(cudaMemsetAsync(d_J, 0, sizeof(double) * (size_t)nbf * nbf, st), "clear J")))

@@ -238,23 +238,26 @@ gbjk_status gbjk_mp2_release(gbjk_ctx* ctx);
 
 /* DF-J for callers that cannot allocate device memory — for example code
  * embedded in a host framework that owns all GPU memory through its own
- * pool, or code that must not allocate while a CUDA graph is captured.
+ * pool and forbids allocations of its own by the libraries it calls.
  * No counterpart in the reference; it is an addition of this engine.
  *
  * Computes the same J as gbjk_compute_j (same kernels, same summation order)
  * without a context: the caller passes the layout (desc: host arrays
- * blk_size and panel_K; desc->colmap is ignored), the panel column map
- * d_colmap, the panels d_B, V^-1 d_Vinv and P_tot d_Ptot in device memory,
- * and receives J in d_J (device, nbf x nbf), all ordered on `stream`.
- * It calls no cudaMalloc/cudaFree and no allocating library routine: all
- * scratch lives in one 16 MiB file-scope device array that every GPU
- * loading the library holds until exit.  Problems whose scratch
- * (nbf*naux + sum_I blk_size[I]*panel_K[I] + 2*naux doubles plus the layout
- * arrays) exceeds 16 MiB, or with naux > 6144, are rejected with
- * GBJK_INVALID_ARG and a message in errbuf.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture.  All calls share the array: calls
- * whose work overlaps on the GPU race and corrupt each other's results. */
+ * blk_size and panel_K, read before the call returns; desc->colmap is
+ * ignored), the panel column map d_colmap, the panels d_B, V^-1 d_Vinv and
+ * P_tot d_Ptot in device memory, and receives J in d_J (device,
+ * nbf x nbf), all ordered on `stream`.  It calls no cudaMalloc/cudaFree and
+ * no allocating library routine: all scratch lives in one 16 MiB file-scope
+ * device array that every GPU loading the library holds until exit.
+ * Problems whose scratch (nbf*naux + sum_I blk_size[I]*panel_K[I] + 2*naux
+ * doubles plus the layout arrays) exceeds 16 MiB, or with naux > 6144,
+ * nbf > 65535 or more than 1024 atom blocks, are rejected with
+ * GBJK_INVALID_ARG and a message in errbuf before anything is launched.
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls share the array and it keeps the last call's contents: calls
+ * whose work may overlap on the GPU race and corrupt each other's results,
+ * so serialise them (one stream, or events between the streams). */
 gbjk_status gbjk_compute_j_noalloc(const gbjk_desc* desc, const int* d_colmap, const double* d_B,
                                    const double* d_Vinv, const double* d_Ptot, double* d_J,
                                    void* stream, char* errbuf, size_t errlen);

@@ -3,8 +3,8 @@
 // set_density_alpha/beta, set_coeff_alpha/beta, set_sym, set_SAD, init(),
 // compute_J()/compute_K(), get_J()/get_K_A()/get_K_B(), and the factories
 // create_j()/create_k() keyed by the same method strings.  Matrices are
-// dense row-major std::vector<double> (the reference passes DBCSR matrices;
-// the binding in INTEGRATION.md converts at the call site).  Errors throw
+// dense row-major std::vector<double> (the reference passes DBCSR matrices,
+// which its call sites convert to and from dense arrays).  Errors throw
 // std::runtime_error carrying gbjk_last_error(), as the reference throws.
 #pragma once
 #include <memory>

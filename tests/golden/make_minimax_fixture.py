@@ -2,8 +2,9 @@
 exponential sums for 1/x on [1, R] (Hackbusch's tables, as shipped with
 megalochem in src/math/laplace/data/init_error.txt, tokens 1_xkKK_RRRR).
 Kept: k <= 10, R <= 1e5, errors >= 3e-9 (the range a double-precision
-Remez iteration resolves).  Run once where the reference tree is present:
-    python tests/golden/make_minimax_fixture.py /root/reference
+Remez iteration resolves).  Run once where the reference tree is present,
+with the root of that tree as the only argument:
+    python tests/golden/make_minimax_fixture.py <megalochem source root>
 """
 import json
 import os
@@ -38,4 +39,6 @@ def main(root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_minimax_fixture.py <megalochem source root>")
+    main(sys.argv[1])

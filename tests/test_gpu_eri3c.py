@@ -30,30 +30,34 @@ def _screened_mask(lay):
     return m
 
 
-@pytest.mark.parametrize("kind,n,dfbasis", [("water", 0, "cc-pvdz-jkfit"),
-                                            ("alkane", 4, "cc-pvdz-jkfit"),
-                                            ("alkane", 2, "cc-pvdz-ri"),
-                                            ("alkane", 10, "cc-pvdz-jkfit")])
-def test_device_eri3c_matches_host(kind, n, dfbasis):
+# (kind, n, auxiliary basis, Schwarz threshold).  At 1e-10 the Schwarz test
+# drops whole AO block pairs only (the panels do not store them); the
+# butane case at 0.1 also screens auxiliary blocks out of two kept AO pairs.
+@pytest.mark.parametrize("kind,n,dfbasis,seps", [("water", 0, "cc-pvdz-jkfit", 1e-10),
+                                                 ("alkane", 4, "cc-pvdz-jkfit", 1e-10),
+                                                 ("alkane", 2, "cc-pvdz-ri", 1e-10),
+                                                 ("alkane", 10, "cc-pvdz-jkfit", 1e-10),
+                                                 ("alkane", 4, "cc-pvdz-jkfit", 0.1)])
+def test_device_eri3c_matches_host(kind, n, dfbasis, seps):
     from chem_gb300.dfsystem import build_dfsystem
     from chem_gb300.fock import JKEngine
     mol = _mol(kind, n, dfbasis)
-    ds = build_dfsystem(mol, eps=1e-10)
-    eng = JKEngine(ds.layout, ("device_ints", mol), np.tril(ds.Linv), ds.Vinv, eps=ds.eps)
+    ds = build_dfsystem(mol, eps=seps)
+    eng = JKEngine(ds.layout, ("device_ints", mol), np.tril(ds.Linv), ds.Vinv, eps=1e-10)
     Bd = eng.download_b()
     scale = np.abs(ds.B).max()
     assert np.abs(Bd - ds.B).max() <= 1e-13 * scale
     # entries of auxiliary blocks screened out for a kept AO block pair are
-    # exactly zero on both (none at this threshold for these molecules:
-    # the Schwarz test drops whole AO pairs, which the panels do not store)
+    # exactly zero on both
     screened = _screened_mask(ds.layout)
+    assert screened.any() == (seps > 1e-3)
     assert not Bd[screened].any() and not ds.B[screened].any()
     # a Fock build on the device tensor matches the host-tensor one
     rng = np.random.default_rng(0)
     C = np.linalg.qr(rng.standard_normal((ds.nbf, ds.nbf)))[0][:, :ds.nocc]
     J1, K1 = eng.compute_jk(2 * C @ C.T, C)
     eng.close()
-    e2 = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=ds.eps)
+    e2 = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=1e-10)
     J2, K2 = e2.compute_jk(2 * C @ C.T, C)
     e2.close()
     # rounding-level tensor differences pass through V^-1 (cond ~1e6 here)

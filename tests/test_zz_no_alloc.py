@@ -1,9 +1,10 @@
 """gbjk_compute_j_noalloc: DF-J for callers that cannot allocate device
-memory (a host framework that owns all GPU memory, or code that must not
-allocate during graph capture).  Compared, through the C ABI, with the
-context-based gbjk_compute_jk on two calls in a row with different
-densities; both run the same kernels in the same order, so the tolerance is
-0 (bit for bit), as in the other FP64 parity tests.
+memory (a host framework that owns all GPU memory through its own pool).
+Compared, through the C ABI, with the context-based gbjk_compute_jk on two
+calls in a row with different densities; both run the same kernels in the
+same order, so the tolerance is 0 (bit for bit), as in the other FP64
+parity tests.  The second call must leave the device's free memory
+unchanged (it allocates nothing).
 
 This file is collected last so that a run stopping at the first failure has
 already run every other test."""
@@ -52,11 +53,14 @@ def test_noalloc_matches_context_path():
         d_P = torch.from_numpy(Ptot).to(dev)
         d_J.fill_(float("nan"))
         torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info(dev)[0]
         err = C.create_string_buffer(256)
         rc = f(C.byref(desc), d_cm.data_ptr(), d_B.data_ptr(), d_V.data_ptr(), d_P.data_ptr(),
                d_J.data_ptr(), None, err, 256)
         assert rc == 0, err.value.decode()
         torch.cuda.synchronize()
+        if call == 1:  # after the first call's one-time set-up: no device memory taken
+            assert torch.cuda.mem_get_info(dev)[0] == free0
         J_ref, _ = eng.compute_jk(Ptot, None)
         J = d_J.cpu().numpy()
         assert np.array_equal(J, J_ref), f"call {call}: max diff {np.abs(J - J_ref).max()}"
@@ -70,4 +74,12 @@ def test_noalloc_matches_context_path():
     rc = f(C.byref(big), d_cm.data_ptr(), d_B.data_ptr(), d_V.data_ptr(), d_P.data_ptr(),
            d_J.data_ptr(), None, err, 256)
     assert rc == 1 and b"limit" in err.value
+    # grids with nbf rows beyond the launch limit are rejected the same way
+    bs_wide = np.array([70000], np.int32)
+    pk_wide = np.array([0], np.int32)
+    wide = GbjkDesc(70000, 8, 1, bs_wide.ctypes.data_as(C.POINTER(C.c_int)),
+                    pk_wide.ctypes.data_as(C.POINTER(C.c_int)), None, 0.0, 0)
+    rc = f(C.byref(wide), d_cm.data_ptr(), d_B.data_ptr(), d_V.data_ptr(), d_P.data_ptr(),
+           d_J.data_ptr(), None, err, 256)
+    assert rc == 1 and b"65535" in err.value
     eng.close()
