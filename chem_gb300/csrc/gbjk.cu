@@ -32,6 +32,10 @@
 
 using namespace gbjk;
 
+// SMs the mixed-path exchange GEMM leaves to the concurrent J column sums
+// unless gbjk_set_overlap says otherwise.
+constexpr int kDefaultOverlapSms = 0;
+
 enum Phase {
   PH_GATHER = 0,
   PH_J_ROWDOT,
@@ -74,6 +78,12 @@ struct CapturedBuild {
 struct gbjk_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  // Mixed-path J column sums run on `side`, forked after the half transform
+  // and joined before the build ends, while the exchange GEMM runs on
+  // `stream` on all SMs but overlap_sms of them (0: no overlap, in order).
+  cudaStream_t side = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int overlap_sms = kDefaultOverlapSms;
   std::string err;
   int64_t launches = 0;
   size_t dev_bytes = 0;
@@ -635,6 +645,12 @@ gbjk_status gbjk_create(gbjk_ctx** out, const gbjk_desc* d) {
     delete ctx;
     return GBJK_CUDA_ERROR;
   }
+  if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    gbjk_destroy(ctx);
+    return GBJK_CUDA_ERROR;
+  }
   gbjk_status s;
   auto up = [&](auto** dptr, const auto& vec) -> gbjk_status {
     gbjk_status st = dalloc(ctx, dptr, vec.size());
@@ -661,6 +677,7 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->side) cudaStreamSynchronize(ctx->side);
   ctx->mp2.release();
   ctx->aok.release();
   ctx->asymk.release();
@@ -681,6 +698,9 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   ctx->user_graph.reset();
   ctx->host_graph.reset();
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->side) cudaStreamDestroy(ctx->side);
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
   delete ctx;
 }
 
@@ -928,6 +948,16 @@ gbjk_status gbjk_download_b(gbjk_ctx* ctx, double* B) {
   return GBJK_OK;
 }
 
+gbjk_status gbjk_set_overlap(gbjk_ctx* ctx, int sms) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (sms < 0 || sms > 128) return fail(ctx, GBJK_INVALID_ARG, "gbjk_set_overlap: 0 <= sms <= 128");
+  if (sms != ctx->overlap_sms) ctx->epoch++;  // the launch sequence changes
+  ctx->overlap_sms = sms;
+  return GBJK_OK;
+}
+
+int gbjk_get_overlap(const gbjk_ctx* ctx) { return ctx ? ctx->overlap_sms : -1; }
+
 gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode) {
   if (!ctx) return GBJK_INVALID_ARG;
   if (jmode != GBJK_J_VINV && jmode != GBJK_J_CHOLESKY)
@@ -976,31 +1006,52 @@ static gbjk_status run_jk_split(gbjk_ctx* ctx, const double* dP, const double* d
                                                              ctx->ncols_total, ctx->d_Cg);
     CKL(PH_GATHER);
   }
-  if ((s = ctx->split.run_k(ctx->stream, dK, &ctx->launches, &ctx->err))) return s;
+  // J = (L^-1 B)^T dt needs only the half transform's density partials: with
+  // overlap on (and no per-phase timing, whose events sit on one stream) it
+  // runs on the side stream beside the exchange
+  const bool fused = dJ && ctx->split.fused_j();
+  const bool overlap = fused && ctx->overlap_sms > 0 && !ctx->profile;
+  ctx->split.ev_ht = overlap ? ctx->ev_fork : nullptr;
+  ctx->split.k_grid = overlap ? ctx->overlap_sms : 0;
+  s = ctx->split.run_k(ctx->stream, dK, &ctx->launches, &ctx->err);
+  ctx->split.ev_ht = nullptr;
+  ctx->split.k_grid = 0;
+  if (s) return s;
+  if (fused) {
+    cudaStream_t js = overlap ? ctx->side : ctx->stream;
+    if (overlap) CK(cudaStreamWaitEvent(js, ctx->ev_fork, 0));
+    CK(cudaMemsetAsync(dJ, 0, (size_t)nbf * nbf * sizeof(double), js));
+    {
+      PhaseScope ps(ctx, PH_J_REDUCE);
+      k_reduce_rows16<<<cdiv(naux, 32), 512, 0, js>>>(ctx->split.d_dpart, nbf, naux,
+                                                      ctx->split.d_dt);
+      CKL(PH_J_REDUCE);
+    }
+    {
+      PhaseScope ps(ctx, PH_J_COLSUM);
+      const int xchunk = kColsumChunk, nchunk = cdiv(naux, xchunk);
+      k_j_colsum_f32x2<<<dim3(cdiv(ctx->maxK, 128), nbf, nchunk), 128, xchunk * sizeof(float2),
+                         js>>>(ctx->split.Bfit, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff,
+                               ctx->d_panelK, ctx->split.d_dt, nbf, naux, xchunk, ctx->maxK,
+                               ctx->d_jpart);
+      k_j_colsum_chunks<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, 0, js>>>(
+          ctx->d_jpart, nchunk, nbf, ctx->maxK, ctx->d_blk_of, ctx->d_panelK, ctx->d_cmoff,
+          ctx->d_colmap, dJ);
+      ctx->launches++;
+      CKL(PH_J_COLSUM);
+    }
+    if (ctx->eps > 0) {
+      PhaseScope ps(ctx, PH_FILTER);
+      k_block_filter<<<dim3(ctx->nblk, ctx->nblk), 128, 0, js>>>(dJ, ctx->nbf, ctx->d_boff,
+                                                                 ctx->eps);
+      CKL(PH_FILTER);
+    }
+    if (overlap) CK(cudaEventRecord(ctx->ev_join, js));
+  }
   if ((s = filter(ctx, dK))) return s;
-  if (!dJ) return GBJK_OK;
-  if (!ctx->split.fused_j()) return run_j(ctx, dP, dJ);  // auxiliary-batched: FP64 J
-  CK(cudaMemsetAsync(dJ, 0, (size_t)nbf * nbf * sizeof(double), ctx->stream));
-  {
-    PhaseScope ps(ctx, PH_J_REDUCE);
-    k_reduce_rows16<<<cdiv(naux, 32), 512, 0, ctx->stream>>>(ctx->split.d_dpart, nbf, naux,
-                                                             ctx->split.d_dt);
-    CKL(PH_J_REDUCE);
-  }
-  {
-    PhaseScope ps(ctx, PH_J_COLSUM);
-    const int xchunk = kColsumChunk, nchunk = cdiv(naux, xchunk);
-    k_j_colsum_f32x2<<<dim3(cdiv(ctx->maxK, 128), nbf, nchunk), 128, xchunk * sizeof(float2),
-                       ctx->stream>>>(ctx->split.Bfit, ctx->d_panel_off, ctx->d_blk_of,
-                                      ctx->d_boff, ctx->d_panelK, ctx->split.d_dt, nbf, naux,
-                                      xchunk, ctx->maxK, ctx->d_jpart);
-    k_j_colsum_chunks<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, 0, ctx->stream>>>(
-        ctx->d_jpart, nchunk, nbf, ctx->maxK, ctx->d_blk_of, ctx->d_panelK, ctx->d_cmoff,
-        ctx->d_colmap, dJ);
-    ctx->launches++;
-    CKL(PH_J_COLSUM);
-  }
-  return filter(ctx, dJ);
+  if (overlap) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_join, 0));
+  if (!dJ || fused) return GBJK_OK;
+  return run_j(ctx, dP, dJ);  // auxiliary-batched: FP64 J
 }
 
 gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, const double* dC,

@@ -19,14 +19,17 @@
 // leading term) and are folded in with 16 fractional bits:
 //   value = 2^(eA+eB-46) (W 2^16 + rint(256 r3) + rint(r4)),
 // where each rint is taken as 32-bit halves with FP32 arithmetic (|256 r3|
-// stays below 2^38 for items of at most 8192 k), and the result is
-// assembled into an FP64 bit pattern with integer operations.
+// stays below 2^38 for items of at most 8192 k); the int64 result is
+// converted to FP64 (round to nearest) and 2^(eA+eB-46) is added to its
+// exponent field.
 //
 // Pipeline (one CTA per SM, persistent over a work list):
 //   warp 0      producer: 1-D bulk copies (cp.async.bulk) of pre-tiled slice
 //               images into a 3-stage shared-memory ring (mbarrier tx count)
 //   warp 1      TMEM allocation and the single MMA-issuing thread
 //   warps 2..13 epilogue: drain exact diagonals per chunk, write results
+//               (row and column exponents loaded at the item start, column
+//               exponents broadcast across the warp by shuffles)
 // Per k-tile the MMA thread issues the exact-diagonal pairs, commits them at
 // a chunk end, then the approximate pairs (15 pairs as 9 MMAs of N = 96 or
 // 192); at a chunk start it issues the approximate pairs first, so the drain
@@ -92,6 +95,19 @@ struct SplitItem {
   // stored in `out` nor counted in emax
   double* out2;
   int c0, ncol1;
+  // Output layout.  perm_rs == 0: row-major out[r * ldr + c].  perm_rs > 0:
+  // the half-transform layout.  The tile's row r is the linear panel row
+  // R = emax_row0 + r = m * perm_div + y (AO function m of the panel,
+  // auxiliary index y); its value in column c lands at
+  //   out[m * perm_rs + (y / 32) * 32 * ldr + (c / 2) * 64 + (y % 32) * 2 + c % 2]
+  // (ldr even, out 16-byte aligned), i.e. within each group of 32 auxiliary
+  // indices the column pairs are outermost.  A warp holds 32 consecutive
+  // rows, so each of its 16-byte column-pair stores is one contiguous
+  // 512-byte run.  Rows of out are flat k-vectors of length perm_rs; a
+  // consumer that contracts over the whole k range (the exchange) needs no
+  // other order, provided every row uses the same one.
+  long long perm_rs = 0;
+  int perm_div = 1;
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -209,8 +225,9 @@ __device__ __forceinline__ void f32_split16(float a, int& h, int& l) {
 }
 
 // v * 2^e2 rounded to nearest FP64, as a bit pattern built with integer
-// operations only (|v| < 2^63).
-__device__ __forceinline__ double i64_scaled_to_f64(long long v, int e2) {
+// operations only (|v| < 2^63); ties round away from zero.  Used where the
+// scaled result leaves the normal range.
+__device__ __forceinline__ double i64_scaled_to_f64_int(long long v, int e2) {
   if (v == 0) return 0.0;
   const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
   const unsigned long long m = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
@@ -233,6 +250,20 @@ __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e2) {
   if (ex <= 0) return 0.0;
   if (ex >= 2047) return __longlong_as_double((long long)(sgn | (0x7FFull << 52)));
   return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | frac));
+}
+
+// v * 2^e2 rounded to nearest FP64 (ties to even): the hardware int64 ->
+// FP64 conversion (exact rounding, one instruction), then e2 added to the
+// exponent field; results below the normal range flush to zero and above it
+// become infinite, as in i64_scaled_to_f64_int.  The epilogue converts
+// 128 x 96 results per work item; this form makes the half transform about
+// 8 % faster than the integer-only one.
+__device__ __forceinline__ double i64_scaled_to_f64(long long v, int e2) {
+  const long long b = __double_as_longlong(__ll2double_rn(v));
+  const int ex = (int)((b >> 52) & 0x7FF) + e2;
+  const long long inf = (b & (1ll << 63)) | (0x7FFll << 52);
+  const long long r = ex <= 0 ? 0ll : (ex >= 2047 ? inf : b + ((long long)e2 << 52));
+  return __longlong_as_double(v == 0 ? 0ll : r);
 }
 
 // ------------------------------------------------------------ split kernels
@@ -275,6 +306,23 @@ __global__ void k_row_maxexp(const SplitJob* __restrict__ jobs) {
 __global__ void k_exp_unbias(int* __restrict__ e, int n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) e[i] = e[i] == 0 ? -2000 : e[i] - 1022;
+}
+
+// Zero the auxiliary slots y0 <= y' < 32 of the last 32-index group of every
+// row of a column-pair-outermost H (SplitItem::perm_rs): rows of rs doubles,
+// the group starting at column gbase, npairs column pairs.  Grid-stride.
+__global__ void k_zero_hpad(double* __restrict__ H, int nrows, long long rs, long long gbase,
+                            int y0, int npairs) {
+  const int ny = 32 - y0;
+  const long long per_row = (long long)npairs * ny;
+  const long long n = (long long)nrows * per_row;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long r = i / per_row, t = i - r * per_row;
+    const long long p = t / ny;
+    const int yy = y0 + (int)(t - p * ny);
+    *reinterpret_cast<double2*>(H + r * rs + gbase + p * 64 + yy * 2) = make_double2(0.0, 0.0);
+  }
 }
 
 __device__ __forceinline__ uint16_t small_int_to_bf16(int d) {
@@ -429,9 +477,6 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool ok = true;
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
         const SplitItem w = items[it];
-        // the epilogue must have read the previous item's d=3,4 accumulators
-        ok = mbar_wait(&final_empty, fin_phase ^ 1, err, 3);
-        fin_phase ^= 1;
         for (int k = 0; k < w.nkt && ok; ++k) {
           const bool chunk_start = (k % kChunkTiles) == 0;
           const bool chunk_end = ((k + 1) % kChunkTiles) == 0 || k + 1 == w.nkt;
@@ -468,7 +513,27 @@ __global__ void __launch_bounds__(kThreads, 1)
               }
             }
           };
-          if (chunk_start) {
+          if (k == 0) {
+            // item start: the exact diagonals are free once the epilogue has
+            // drained the previous item's last chunk, which comes before its
+            // fold of d = 3, 4; so the exact pairs go first and overlap that
+            // fold, and the d = 3, 4 pairs wait for it
+            ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4);
+            ex_phase ^= 1;
+            if (!ok) {
+              mma_commit(&empty_bar[stage]);  // the ring drain still completes
+              break;
+            }
+            issue(0, 4);
+            if (chunk_end) mma_commit(&exact_full);
+            ok = mbar_wait(&final_empty, fin_phase ^ 1, err, 3);
+            fin_phase ^= 1;
+            if (!ok) {
+              mma_commit(&empty_bar[stage]);
+              break;
+            }
+            issue(4, 9);
+          } else if (chunk_start) {
             // d = 3, 4 first: they accumulate over the whole item and the
             // exact drain does not read them, so they overlap the epilogue's
             // drain of the previous chunk; the exact pairs wait for it
@@ -504,7 +569,14 @@ __global__ void __launch_bounds__(kThreads, 1)
     uint32_t ex_phase = 0, fin_phase = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
-      const SplitItem w = items[it];
+      const SplitItem& w = items[it];  // fields read where used (register pressure)
+      // row exponent of this thread's row and the column exponents of the
+      // warp's 32 columns (one per lane, broadcast by shuffles at the store),
+      // loaded now so that their latency hides behind the drains; a tile's
+      // 128 A rows and 96 B rows are always allocated
+      const int cbase = half * kEpiCols;
+      const int er = w.ea[row];
+      const int ecl = w.eb[cbase + lane];
       long long V[kEpiCols];
 #pragma unroll
       for (int c = 0; c < kEpiCols; ++c) V[c] = 0;
@@ -562,37 +634,58 @@ __global__ void __launch_bounds__(kThreads, 1)
       tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&final_empty);
-      const bool rvalid = row < w.m_valid;
+      // item fields of the store phase, loaded together so their latencies
+      // overlap
+      const int m_valid = w.m_valid, n_valid = w.n_valid, ncol1 = w.ncol1, c0 = w.c0;
+      const int emax_row0 = w.emax_row0, emax_div = w.emax_div, perm_div = w.perm_div;
+      double* const out = w.out;
+      double* const out2 = w.out2;
+      const long long ldr = w.ldr, perm_rs = w.perm_rs;
+      const bool rvalid = row < m_valid;
       unsigned int emax_row = 0;
-      if (rvalid) {
-        const int er = w.ea[row];
-        double* orow = w.out + (long long)row * w.ldr + half * kEpiCols;
-        const int cbase = half * kEpiCols;
+      {
+        const bool perm = perm_rs != 0;
+        double* orow;
+        if (perm) {
+          const int R = emax_row0 + row;
+          const int m = R / perm_div, y = R - m * perm_div;
+          orow = out + (long long)m * perm_rs + (long long)(y & ~31) * ldr +
+                 ((y & 31) * 2 + (cbase >> 1) * 64);
+        } else {
+          orow = out + (long long)row * ldr + cbase;
+        }
         const bool vec = ((uintptr_t)orow & 15) == 0;
-        const int nstore = min(w.n_valid, w.ncol1 - w.c0);  // columns kept in `out`
+        const int nstore = min(n_valid, ncol1 - c0);  // columns kept in `out`
         // density column of this row's AO function (tile-local), or -1
         int dcol = -1;
-        if (w.out2) {
-          const int cand = w.ncol1 + (w.emax_row0 + row) / w.emax_div - w.c0;
-          if (cand >= 0 && cand < w.n_valid) dcol = cand;
+        if (out2) {
+          const int cand = ncol1 + (emax_row0 + row) / emax_div - c0;
+          if (cand >= 0 && cand < n_valid) dcol = cand;
         }
 #pragma unroll
         for (int c = 0; c < kEpiCols; c += 2) {
+          const int ecs0 = __shfl_sync(0xffffffffu, ecl, c);
+          const int ecs1 = __shfl_sync(0xffffffffu, ecl, c + 1);
           const int col = cbase + c;
-          const bool s0 = col < nstore, s1 = col + 1 < nstore;
-          const bool d0 = col == dcol, d1 = col + 1 == dcol;
+          const bool s0 = rvalid && col < nstore, s1 = rvalid && col + 1 < nstore;
+          const bool d0 = rvalid && col == dcol, d1 = rvalid && col + 1 == dcol;
           if (!(s0 || s1 || d0 || d1)) continue;
-          const int ec0 = (s0 || d0) ? w.eb[col] : -2000;
-          const int ec1 = (s1 || d1) ? w.eb[col + 1] : -2000;
+          const int ec0 = (s0 || d0) ? ecs0 : -2000;
+          const int ec1 = (s1 || d1) ? ecs1 : -2000;
           const double x0 =
               (er <= -2000 || ec0 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c], er + ec0 - 46);
           const double x1 =
               (er <= -2000 || ec1 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c + 1], er + ec1 - 46);
-          if (d0) w.out2[w.emax_row0 + row] = x0;
-          if (d1) w.out2[w.emax_row0 + row] = x1;
+          if (d0) out2[emax_row0 + row] = x0;
+          if (d1) out2[emax_row0 + row] = x1;
           if (s0) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x0) >> 52) & 0x7FF));
           if (s1) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x1) >> 52) & 0x7FF));
-          if (vec && s0 && s1) {
+          if (perm) {
+            // the pair's second column is the zero pad column when nstore
+            // is odd (the last orbital of an odd count)
+            if (s0)
+              *reinterpret_cast<double2*>(orow + (c >> 1) * 64) = make_double2(x0, s1 ? x1 : 0.0);
+          } else if (vec && s0 && s1) {
             *reinterpret_cast<double2*>(orow + c) = make_double2(x0, x1);
           } else {
             if (s0) orow[c] = x0;
@@ -600,18 +693,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           }
         }
       }
-      if (w.emax) {
+      if (unsigned int* const emaxp = w.emax) {
         // one atomic per warp when all its rows map to the same target row
-        const int target = rvalid ? (w.emax_row0 + row) / w.emax_div : -1;
+        const int target = rvalid ? (emax_row0 + row) / emax_div : -1;
         const int t0 = __shfl_sync(0xffffffffu, target, 0);
         const bool same = __all_sync(0xffffffffu, target == t0);
         if (same) {
           unsigned int m = emax_row;
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-          if (lane == 0 && t0 >= 0 && m) atomicMax(w.emax + t0, m);
+          if (lane == 0 && t0 >= 0 && m) atomicMax(emaxp + t0, m);
         } else if (target >= 0 && emax_row) {
-          atomicMax(w.emax + target, emax_row);
+          atomicMax(emaxp + target, emax_row);
         }
       }
     }

@@ -67,6 +67,11 @@ struct SplitState {
   int nsm = 148;
   bool attr_set = false;
   bool profile = false;
+  // set by the caller for one build: event recorded right after the half
+  // transform (the fork point of the J column sums), and the number of SMs
+  // the exchange GEMM leaves free (0: all SMs)
+  cudaEvent_t ev_ht = nullptr;
+  int k_grid = 0;
   double ms[4] = {0, 0, 0, 0};
   int64_t nl[4] = {0, 0, 0, 0};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -181,9 +186,13 @@ struct SplitState {
   };
 
   static int cdiv_(long long a, long long b) { return (int)((a + b - 1) / b); }
+  // H rows hold the half transform in groups of 32 auxiliary indices (the
+  // column-pair-outermost layout of SplitItem::perm_rs), so a batch of xbc
+  // auxiliary rows spans pad32(xbc) * hld columns of H
+  static int pad32(int x) { return (x + 31) & ~31; }
 
   gbjk_status launch_gemm(cudaStream_t st, SplitItem* items, int n, int64_t* launches,
-                          std::string* err) {
+                          std::string* err, int leave_sms = 0) {
     if (n == 0) return GBJK_OK;
     if (!attr_set) {
       if (cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -196,7 +205,7 @@ struct SplitState {
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
       attr_set = true;
     }
-    const int grid = std::min(n, nsm);
+    const int grid = std::min(n, std::max(1, nsm - leave_sms));
     k_split_gemm<<<grid, kThreads, kSmemBytes, st>>>(items, n, d_err);
     (*launches)++;
     cudaError_t e = cudaGetLastError();
@@ -215,7 +224,10 @@ struct SplitState {
       *err = "split path: cannot allocate the error flag";
       return GBJK_OOM;
     }
-    xb = (xb_req > 0 && xb_req < naux) ? xb_req : naux;
+    // batches of a multiple of 32 auxiliary rows, so that only the last
+    // (shorter) batch has unused slots in its last 32-index group of H
+    xb = (xb_req > 0 && xb_req < naux) ? std::max(32, xb_req & ~31) : naux;
+    if (xb > naux) xb = naux;
     nbatch = (naux + xb - 1) / xb;
     double* d_Bfit = nullptr;
     if (fitted) {
@@ -410,7 +422,7 @@ struct SplitState {
       ctot += (long long)c_nrb * nkt[I] * kSlices * kImage;
     }
     hld = nocc_ + (nocc_ & 1);  // even row stride: 16-byte aligned pairs
-    const long long hk = (long long)xb * hld;
+    const long long hk = (long long)pad32(xb) * hld;
     h_nkt = cdiv_(hk, kTileK);
     h_nrb = std::max(cdiv_(nbf, kTileM) * (kTileM / 32), cdiv_(nbf, kTileN) * (kTileN / 32));
     int dev = 0;
@@ -424,7 +436,8 @@ struct SplitState {
     const int xlast = naux - (nbatch - 1) * xb;
     if (xlast != xb) sizes.push_back(xlast);
     ksplit = 1;
-    for (int xbc : sizes) ksplit = std::max(ksplit, choose_ksplit(cdiv_((long long)xbc * hld, kTileK), ntile));
+    for (int xbc : sizes)
+      ksplit = std::max(ksplit, choose_ksplit(cdiv_((long long)pad32(xbc) * hld, kTileK), ntile));
     if (alloc(&d_Cslices, (size_t)ctot) != cudaSuccess ||
         alloc(&d_eC, (size_t)nblk * c_nrb * 32) != cudaSuccess ||
         alloc(&d_H, (size_t)nbf * hk) != cudaSuccess ||
@@ -467,9 +480,12 @@ struct SplitState {
             w.nkt = nkt[I];
             w.ea = d_eA + eA_off[I] + (long long)mt * kTileM;
             w.eb = d_eC + (long long)I * c_nrb * 32 + (long long)nt * kTileN;
-            w.out = d_H + ((long long)boff[I] * xbc + (long long)mt * kTileM) * hld +
-                    (long long)nt * kTileN;
+            // column-pair-outermost layout: each epilogue store is one
+            // contiguous 512-byte run (SplitItem::perm_rs)
+            w.out = d_H + (long long)boff[I] * pad32(xbc) * hld + (long long)nt * kTileN * 32;
             w.ldr = hld;
+            w.perm_rs = (long long)pad32(xbc) * hld;
+            w.perm_div = xbc;
             w.m_valid = (int)std::min<long long>(kTileM, rows - (long long)mt * kTileM);
             w.n_valid = std::min(kTileN, ncolI - nt * kTileN);
             // row (m, y) of panel I belongs to H row mu = boff[I] + m
@@ -485,7 +501,7 @@ struct SplitState {
       }
       pl.nht = (int)items.size() - pl.ht0;
       // exchange: upper tiles, split over k
-      const int nk_b = cdiv_((long long)xbc * hld, kTileK);
+      const int nk_b = cdiv_((long long)pad32(xbc) * hld, kTileK);
       const int ksb = choose_ksplit(nk_b, ntile);
       const int kt_per = cdiv_(nk_b, ksb);
       pl.ksplit = cdiv_(nk_b, kt_per);
@@ -525,11 +541,11 @@ struct SplitState {
       // digits of the half-transformed batch (exponents from the epilogue)
       SplitJob hj;
       hj.src = d_H;
-      hj.rs = (long long)xbc * hld;
+      hj.rs = (long long)pad32(xbc) * hld;
       hj.cs = 1;
       hj.row0 = 0;
       hj.nrows = nbf;
-      hj.ncols = (long long)xbc * hld;
+      hj.ncols = (long long)pad32(xbc) * hld;
       hj.e = d_eH;
       hj.e_biased = 0;
       hj.nrb = h_nrb;
@@ -627,6 +643,16 @@ struct SplitState {
         k_split_tiles<<<dim3(cdiv_((long long)bjob_maxthr, 256), nbf), 256, 0, st>>>(bj);
         *launches += 2;
       }
+      if (nbatch > 1 && pad32(pl.xbc) != pl.xbc) {
+        // the last batch's H layout reuses slots the full batches wrote:
+        // clear its unused auxiliary slots
+        Scope sc(this, 2, st);
+        const long long per = (long long)nbf * (hld / 2) * (32 - (pl.xbc & 31));
+        k_zero_hpad<<<(int)std::min<long long>(cdiv_(per, 256), 4LL * nsm), 256, 0, st>>>(
+            d_H, nbf, (long long)pad32(pl.xbc) * hld, (long long)(pl.xbc & ~31) * hld,
+            pl.xbc & 31, hld / 2);
+        (*launches)++;
+      }
       {
         Scope sc(this, 0, st);
         // H row exponents are atomically maximised by the half-transform epilogue
@@ -636,16 +662,21 @@ struct SplitState {
         }
         if ((s = launch_gemm(st, d_items + pl.ht0, pl.nht, launches, err))) return s;
       }
+      if (ev_ht && nbatch == 1 && cudaEventRecord(ev_ht, st) != cudaSuccess) {
+        *err = "split path: event record failed";
+        return GBJK_CUDA_ERROR;
+      }
       {
         Scope sc(this, 2, st);
         k_exp_unbias<<<cdiv_((long long)h_nrb * 32, 256), 256, 0, st>>>(d_eH, h_nrb * 32);
-        const long long hthr = (long long)(nbf / 8 + 2) * cdiv_((long long)pl.xbc * hld, kTileK) * 32;
+        const long long hthr =
+            (long long)(nbf / 8 + 2) * cdiv_((long long)pad32(pl.xbc) * hld, kTileK) * 32;
         k_split_tiles<<<dim3(cdiv_(hthr, 256), 1), 256, 0, st>>>(d_jobs + pl.hjob);
         *launches += 2;
       }
       {
         Scope sc(this, 1, st);
-        if ((s = launch_gemm(st, d_items + pl.k0, pl.nk, launches, err))) return s;
+        if ((s = launch_gemm(st, d_items + pl.k0, pl.nk, launches, err, k_grid))) return s;
       }
       k_splitk_reduce_acc<<<cdiv_((long long)nbf * nbf, 256), 256, 0, st>>>(
           d_Kpart, pl.ksplit, nbf, -1.0, 1, b > 0 ? 1 : 0, dK);

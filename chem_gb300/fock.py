@@ -63,6 +63,9 @@ def lib():
         L.gbjk_upload_metric.argtypes = [vp, dp, dp]
         L.gbjk_set_precision.argtypes = [vp, C.c_int, C.c_int]
         L.gbjk_set_jmode.argtypes = [vp, C.c_int]
+        L.gbjk_set_overlap.argtypes = [vp, C.c_int]
+        L.gbjk_get_overlap.argtypes = [vp]
+        L.gbjk_get_overlap.restype = C.c_int
         L.gbjk_set_fitted.argtypes = [vp, C.c_int]
         L.gbjk_set_aux_batch.argtypes = [vp, C.c_int]
         L.gbjk_upload_b_synthetic.argtypes = [vp, C.c_ulonglong, C.c_double]
@@ -210,6 +213,14 @@ class JKEngine:
         B = np.empty(self.layout.nnz)
         self._check(lib().gbjk_download_b(self.h, _dp(B)), "gbjk_download_b")
         return B
+
+    def set_overlap(self, sms):
+        """SMs the mixed-path exchange leaves to the concurrent J column
+        sums (0: phases in order on one stream)."""
+        self._check(lib().gbjk_set_overlap(self.h, int(sms)), "gbjk_set_overlap")
+
+    def get_overlap(self):
+        return int(lib().gbjk_get_overlap(self.h))
 
     def set_jmode(self, jmode):
         """'vinv' (reference route, default) or 'cholesky'."""

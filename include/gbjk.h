@@ -98,7 +98,7 @@ gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices);
  * No counterpart in the reference. */
 gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted);
 /* Split path: process the auxiliary index in batches of `rows` (0 = all at
- * once), streaming the half transform and the exchange batch by batch so
+ * once; rounded down to a multiple of 32, at least 32), streaming the half transform and the exchange batch by batch so
  * that the half-transformed tensor never exists in full.  No counterpart in
  * the reference (it batches over X with DBCSR, src/fock/jkdf.cpp:412-422). */
 gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows);
@@ -134,6 +134,14 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
                                 const int* ablk_shell_off, int npairs, const int* pair_I,
                                 const int* pair_J, const unsigned char* keep, const int* col_IJ,
                                 const int* col_JI);
+
+/* Mixed-precision build: after the half transform the J column sums
+ * (HBM-bound) run on a second stream of the context beside the exchange
+ * GEMM (tensor-bound), which then leaves `sms` SMs to them; 0 runs the
+ * phases in order on one stream.  Results are the same bits either way.
+ * No counterpart in the reference. */
+gbjk_status gbjk_set_overlap(gbjk_ctx* ctx, int sms);
+int gbjk_get_overlap(const gbjk_ctx* ctx);
 
 /* jmode: GBJK_J_VINV (default, the reference route) or GBJK_J_CHOLESKY.
  * No counterpart in the reference. */
