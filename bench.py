@@ -573,6 +573,7 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
 
+    from chem_gb300 import accuracy
     from chem_gb300.fock import JKEngine, host_array, k_split_plan
 
     mol, ds, Cocc, P, tset = setup(args.alkane)
@@ -739,6 +740,18 @@ def main():
         Jfc, _ = eng.compute_jk(Ph, None, args.kmethod)
         eng.set_jmode("vinv")
         eng.set_precision(args.precision)
+        # Coulomb energy of each route against the exactly refined solve of
+        # V h = g (quadruple-precision residuals where numpy has them)
+        cexact = None
+        if accuracy.have_quad():
+            g = accuracy.panel_g(ds.layout, ds.B, 2.0 * P)
+            cr = accuracy.coulomb_routes(ds.V, ds.Linv, ds.Vinv, g, residual="quad")
+            cexact = {"E_J_exact_Eh": cr["E_exact"],
+                      "mixed": accuracy.j_energy_vs_exact(P, Jm, cr["E_exact"]),
+                      "fp64_vinv_route": accuracy.j_energy_vs_exact(P, Jf, cr["E_exact"]),
+                      "fp64_cholesky_route": accuracy.j_energy_vs_exact(P, Jfc, cr["E_exact"]),
+                      "definition": "sum P_alpha J - 1/2 g^T V^-1 g, the exact solve by "
+                                    "iterative refinement with quadruple-precision residuals"}
         fp64 = {"value": world * 1e3 / ms64, "unit": "builds/s", "ms_per_step": ms64,
                 "steps": nst,
                 "speedup_mixed_over_fp64": ms64 / ms,
@@ -748,6 +761,7 @@ def main():
                 "dE_K_Eh": float(np.sum(P * (Km - Kf))),
                 "max_abs_dJ_vs_fp64_cholesky": float(np.abs(Jm - Jfc).max()),
                 "dE_vs_fp64_cholesky_Eh": float(np.sum(P * ((Jm - Jfc) + (Km - Kf)))),
+                "coulomb_energy_vs_exact_Eh": cexact,
                 "fp64_route_note": "fp64 J uses the explicit V^-1 of fock::DF_J; for this "
                                    "metric (cond ~2e7) that route itself errs by ~1e-6 Eh in "
                                    "the Coulomb energy, the Cholesky route by ~1e-10 Eh",
@@ -817,44 +831,75 @@ def main():
     # (Cholesky route) once the DIIS error is below 1e-5
     scf = None
     if not args.no_scf:
-        from chem_gb300.scf import run_rhf
+        from chem_gb300.scf import fp64_switch, run_rhf
 
-        def run(prec, jmode, switch):
+        def jk(Pa, Ca):
+            return eng.compute_jk(2.0 * Pa, Ca, args.kmethod)
+
+        def run(prec, jmode, switch_route=None, audit=None, max_vecs=8):
             eng.set_precision(prec)
             eng.set_jmode(jmode)
-
-            def jk(Pa, Ca):
-                return eng.compute_jk(2.0 * Pa, Ca, args.kmethod)
-
-            sw = None
-            if switch:
-                def sw():
-                    eng.set_precision("fp64")
+            sw = fp64_switch(eng, switch_route) if switch_route else None
             t0 = time.perf_counter()
             r = run_rhf(ds.S, ds.Hcore, mol.nuclear_repulsion(), mol.nocc, jk, conv=1e-8,
-                        switch=sw)
+                        switch=sw, audit=audit, max_vecs=max_vecs)
             return r, time.perf_counter() - t0
 
-        r_ref, t_ref = run("fp64", "vinv", False)
-        r_chol, t_chol = run("fp64", "cholesky", False)
-        r_mix, t_mix = run("split", "cholesky", True)
-        r_pure, t_pure = run("split", "cholesky", False)
+        def e_exact_metric(r):
+            # energy of a converged state with J on the Cholesky route
+            eng.set_precision("fp64")
+            eng.set_jmode("cholesky")
+            J, K = jk(r.P, r.C[:, :mol.nocc])
+            return float(np.sum(r.P * (2 * ds.Hcore + J + K)) + mol.nuclear_repulsion())
+
+        def rec(r, t, **kw):
+            return dict({"E": r.energy, "iterations": r.iterations, "seconds": round(t, 2),
+                         "converged": r.converged}, **kw)
+
+        def audit(Pa, Ca, J, K):
+            # every mixed build against an FP64 (Cholesky route) build at the
+            # same density
+            eng.set_precision("fp64")
+            eng.set_jmode("cholesky")
+            J64, K64 = jk(Pa, Ca)
+            eng.set_precision("split")
+            return (float(np.abs(K - K64).max()), float(np.sum(Pa * ((J - J64) + (K - K64)))))
+
+        r_ref, t_ref = run("fp64", "vinv")
+        r_chol, t_chol = run("fp64", "cholesky")
+        r_mix, t_mix = run("split", "cholesky", "cholesky")
+        r_mixv, t_mixv = run("split", "cholesky", "vinv")
+        r_pure, t_pure = run("split", "cholesky")
+        r_aud, _ = run("split", "cholesky", audit=audit)
+        r_ref6, t_ref6 = run("fp64", "vinv", max_vecs=6)
+        ec = {"fp64_vinv_route": e_exact_metric(r_ref),
+              "fp64_vinv_route_diis6": e_exact_metric(r_ref6),
+              "mixed_then_fp64_vinv": e_exact_metric(r_mixv)}
         eng.set_precision(args.precision)
         eng.set_jmode("vinv")
+        sw_note = "FP64 once the DIIS RMS error < 1e-5"
         scf = {"conv_rms": 1e-8,
-               "fp64_vinv_route": {"E": r_ref.energy, "iterations": r_ref.iterations,
-                                   "seconds": round(t_ref, 2), "converged": r_ref.converged},
-               "fp64_cholesky_route": {"E": r_chol.energy, "iterations": r_chol.iterations,
-                                       "seconds": round(t_chol, 2),
-                                       "converged": r_chol.converged},
-               "mixed_then_fp64": {"E": r_mix.energy, "iterations": r_mix.iterations,
-                                   "seconds": round(t_mix, 2), "converged": r_mix.converged,
-                                   "switch": "FP64 once the DIIS RMS error < 1e-5"},
-               "mixed_only": {"E": r_pure.energy, "iterations": r_pure.iterations,
-                              "seconds": round(t_pure, 2), "converged": r_pure.converged},
+               "fp64_vinv_route": rec(r_ref, t_ref),
+               "fp64_cholesky_route": rec(r_chol, t_chol),
+               "mixed_then_fp64_cholesky": rec(r_mix, t_mix, switch=sw_note + ", Cholesky route"),
+               "mixed_then_fp64_vinv": rec(r_mixv, t_mixv, switch=sw_note + ", V^-1 route"),
+               "mixed_only": rec(r_pure, t_pure),
                "dE_mixed_only_vs_fp64_cholesky": r_pure.energy - r_chol.energy,
-               "dE_mixed_then_fp64_vs_fp64_cholesky": r_mix.energy - r_chol.energy,
-               "dE_fp64_vinv_vs_cholesky": r_ref.energy - r_chol.energy}
+               "dE_mixed_then_fp64_cholesky_vs_fp64_cholesky": r_mix.energy - r_chol.energy,
+               "dE_mixed_then_fp64_vinv_vs_fp64_vinv": r_mixv.energy - r_ref.energy,
+               "dE_fp64_vinv_vs_cholesky": r_ref.energy - r_chol.energy,
+               "fp64_vinv_route_diis6": rec(r_ref6, t_ref6),
+               "vinv_route_restart_spread_Eh": r_ref6.energy - r_ref.energy,
+               "vinv_route_states_exact_metric_E": ec,
+               "vinv_route_note": "the V^-1 route's converged energy carries the explicit "
+                                  "inverse's rounding noise, different for every SCF "
+                                  "trajectory (see the restart spread); its converged "
+                                  "states are compared by their exact-metric energies",
+               "mixed_only_per_build_vs_fp64_cholesky": {
+                   "max_abs_dK": [a[0] for a in r_aud.audit],
+                   "dE_Eh": [a[1] for a in r_aud.audit],
+                   "worst_max_abs_dK": max(a[0] for a in r_aud.audit),
+                   "worst_abs_dE_Eh": max(abs(a[1]) for a in r_aud.audit)}}
 
     out = {
         "metric": METRIC, "value": value, "unit": "builds/s", "n_gpus": world,

@@ -15,7 +15,10 @@ iterative refinement with exactly computed residuals:
     correction d_k solves V d_k = r_{k-1} with the FP64 Cholesky factor.
 Each step shrinks the error by about cond(V) * 2^-53, so three steps give
 the exact solution far beyond FP64 resolution.  Energies gᵀh are summed the
-same way.  No GPU; used by the tests and the bench's accuracy report.
+same way.  Where numpy's longdouble is IEEE quadruple precision (aarch64),
+the residuals can instead be formed in quad arithmetic, which is much faster
+for naux in the thousands.  No GPU; used by the tests and the bench's
+accuracy report.
 """
 from __future__ import annotations
 
@@ -66,17 +69,37 @@ def exact_residual(V, g, parts):
     return r
 
 
-def refined_solve(V, g, steps=3):
+def quad_residual(V, g, parts):
+    """r = g - V (sum_k parts[k]) in IEEE quadruple precision (numpy
+    longdouble where it has a 113-bit significand, as on aarch64), rounded
+    to FP64 at the end.  Its error, ~2^-113 of the terms, is far below what
+    refinement needs for cond(V) ~ 1e7."""
+    ld = np.longdouble
+    Vq = V.astype(ld)
+    h = np.zeros(len(g), ld)
+    for p in parts:
+        h += p.astype(ld)
+    return (g.astype(ld) - Vq @ h).astype(np.float64)
+
+
+def have_quad():
+    return np.finfo(np.longdouble).nmant >= 112
+
+
+def refined_solve(V, g, steps=3, residual=None):
     """The solution of V h = g as a list of FP64 vectors whose exact sum
     is h to far beyond FP64 resolution (iterative refinement with exact
-    residuals).  Returns (parts, residual norm after the last step)."""
+    residuals: correctly rounded sums, or quadruple precision where numpy
+    has it and residual="quad").  Returns (parts, residual norm after the
+    last step)."""
+    res = quad_residual if residual == "quad" else exact_residual
     cf = sla.cho_factor(V, lower=True)
     parts = [sla.cho_solve(cf, g)]
     r = None
     for _ in range(steps):
-        r = exact_residual(V, g, parts)
+        r = res(V, g, parts)
         parts.append(sla.cho_solve(cf, r))
-    r = exact_residual(V, g, parts)
+    r = res(V, g, parts)
     return parts, float(np.abs(r).max())
 
 
@@ -113,11 +136,13 @@ def panel_j(layout, B, h):
     return J
 
 
-def coulomb_routes(V, Linv, Vinv, g):
+def coulomb_routes(V, Linv, Vinv, g, residual=None):
     """Coulomb energy E_J = 1/2 gᵀV⁻¹g (Eh, for g from P_tot = 2 P_alpha)
     exactly and on the two FP64 routes, plus each route's h and the exact h
-    rounded to FP64.  Linv is the lower-triangular L^-1 with V = L Lᵀ."""
-    parts, res = refined_solve(V, g)
+    rounded to FP64.  Linv is the lower-triangular L^-1 with V = L Lᵀ.
+    residual="quad" refines with quadruple-precision residuals (fast where
+    numpy's longdouble is IEEE quad); the default sums exactly."""
+    parts, res = refined_solve(V, g, residual=residual)
     e_exact = 0.5 * exact_dot(g, parts)
     h_exact = np.sum(parts, axis=0)  # rounded to FP64
     h_vinv = Vinv @ g

@@ -33,6 +33,7 @@ class SCFResult:
     P: np.ndarray
     F: np.ndarray
     history: list = field(default_factory=list)
+    audit: list = field(default_factory=list)
 
 
 class DIIS:
@@ -64,18 +65,32 @@ class DIIS:
         return sum(ci * Fi for ci, Fi in zip(c, self.F))
 
 
+def fp64_switch(engine, jmode="cholesky"):
+    """Switch callback for run_rhf: moves a split-precision engine to the
+    FP64 path with J on the given route ("cholesky", or "vinv" for the
+    reference's explicit V^-1)."""
+    def sw():
+        engine.set_precision("fp64")
+        engine.set_jmode(jmode)
+    return sw
+
+
 def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max_vecs=8,
-            switch=None, switch_thresh=1e-5, log=None):
+            switch=None, switch_thresh=1e-5, log=None, audit=None):
     """jk(P_alpha, C_occ) -> (J, K_alpha) with K already negated; conv is the
     RMS threshold of the error matrix (megalochem's scf_thresh).
     switch(): called once when the DIIS RMS error falls below switch_thresh
-    (moves a split-precision engine to FP64)."""
+    (moves a split-precision engine to FP64, e.g. fp64_switch(engine)).
+    audit(P_alpha, C_occ, J, K) -> dict: called on every build's result
+    (e.g. its deviation from an FP64 build at the same density); the dicts
+    are returned in SCFResult.audit, one per iteration."""
     s, U = np.linalg.eigh(S)
     X = U @ np.diag(s ** -0.5) @ U.T
     F = Hcore.copy()
     diis = DIIS(max_vecs)
     E_old = 0.0
     hist = []
+    audits = []
     switched = switch is None
     for it in range(max_iter):
         Fo = X.T @ F @ X
@@ -84,6 +99,8 @@ def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max
         Cocc = Cm[:, :nocc]
         P = Cocc @ Cocc.T
         J, K = jk(P, Cocc)
+        if audit is not None:
+            audits.append(audit(P, Cocc, J, K))
         F_new = Hcore + J + K
         E = float(np.sum(P * (Hcore + F_new)) + enuc)
         err = F_new @ P @ S - S @ P @ F_new
@@ -98,11 +115,11 @@ def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max
             F = F_new
             continue
         if it > 0 and rms < conv and switched:
-            return SCFResult(E, True, it + 1, Cm, e, P, F_new, hist)
+            return SCFResult(E, True, it + 1, Cm, e, P, F_new, hist, audits)
         E_old = E
         if it >= diis_start:
             diis.push(F_new, err)
             F = diis.extrapolate()
         else:
             F = F_new
-    return SCFResult(E, False, max_iter, Cm, e, P, F_new, hist)
+    return SCFResult(E, False, max_iter, Cm, e, P, F_new, hist, audits)

@@ -51,3 +51,14 @@ def decane():
     s, x = geometry.alkane(10)
     mol = molecule_from_angstrom(s, x, "cc-pvdz", "cc-pvdz-jkfit")
     return build_dfsystem(mol, eps=1e-10)
+
+
+@pytest.fixture(scope="session")
+def c20h42():
+    """n-C20H42, the benchmark molecule (nbf 490, naux 2366, nocc 81)."""
+    from chem_gb300 import geometry
+    from chem_gb300.dfsystem import build_dfsystem
+    from chem_gb300.molecule import molecule_from_angstrom
+    s, x = geometry.alkane(20)
+    mol = molecule_from_angstrom(s, x, "cc-pvdz", "cc-pvdz-jkfit")
+    return build_dfsystem(mol, eps=1e-10)

@@ -69,3 +69,22 @@ def test_cholesky_route_is_exact_vinv_route_is_not(fixture, vinv_min, request):
     dj_chol = np.abs(J_chol - J_exact).max()
     dj_vinv = np.abs(J_vinv - J_exact).max()
     assert dj_chol <= 1e-10 and dj_vinv >= 10 * dj_chol
+
+
+@pytest.mark.skipif(not __import__("chem_gb300.accuracy", fromlist=["x"]).have_quad(),
+                    reason="numpy longdouble is not IEEE quadruple precision here")
+def test_quad_residual_matches_exact_sums():
+    """Where numpy's longdouble is IEEE quad (aarch64), the faster quad
+    residuals give the same refined energy as the exactly summed ones."""
+    from chem_gb300 import accuracy
+    rng = np.random.default_rng(5)
+    n = 80
+    Q = np.linalg.qr(rng.standard_normal((n, n)))[0]
+    V = Q @ np.diag(np.logspace(0, -7, n)) @ Q.T
+    V = 0.5 * (V + V.T)
+    g = rng.standard_normal(n)
+    pe, _ = accuracy.refined_solve(V, g)
+    pq, res = accuracy.refined_solve(V, g, residual="quad")
+    assert res < 1e-25
+    e1, e2 = accuracy.exact_dot(g, pe), accuracy.exact_dot(g, pq)
+    assert abs(e1 - e2) <= 1e-14 * abs(e1)
