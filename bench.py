@@ -588,7 +588,10 @@ def main():
     torch.cuda.synchronize()
     stream = torch.cuda.ExternalStream(eng.stream, device=dev)
 
-    # the whole Fock build (all launches, memsets) is one CUDA graph
+    # launch choices of this problem picked by the autotuner (timed here,
+    # no cache file), then the whole Fock build (all launches, memsets) is
+    # one CUDA graph
+    tune = eng.autotune(2.0 * P, Cocc, args.kmethod, reps=10)
     eng.capture_graph(dP.data_ptr(), dC.data_ptr(), mol.nocc, dJ.data_ptr(), dK.data_ptr(),
                       args.kmethod)
 
@@ -722,6 +725,7 @@ def main():
     if args.precision == "split" and not args.no_fp64_compare:
         Jm, Km = eng.compute_jk(Ph, Cocc, args.kmethod)
         eng.set_precision("fp64")
+        tune64 = eng.autotune(2.0 * P, Cocc, args.kmethod, reps=1)
         eng.compute_jk(Ph, Cocc, args.kmethod)
         nst = max(2, min(args.steps, 5))
         torch.cuda.synchronize()
@@ -753,6 +757,8 @@ def main():
                       "definition": "sum P_alpha J - 1/2 g^T V^-1 g, the exact solve by "
                                     "iterative refinement with quadruple-precision residuals"}
         fp64 = {"value": world * 1e3 / ms64, "unit": "builds/s", "ms_per_step": ms64,
+                "autotune": {"chosen": tune64["chosen"], "best_ms": tune64["best_ms"],
+                             "candidates": len(tune64["candidates"])},
                 "steps": nst,
                 "speedup_mixed_over_fp64": ms64 / ms,
                 "max_abs_dK": float(np.abs(Km - Kf).max()),
@@ -908,7 +914,10 @@ def main():
         "dtype": "f64 in/out; bf16 digit slices x5 on tcgen05, exact int64 recombination"
                  if args.precision == "split" else "f64",
         "data": "synthetic molecule (seed-free alkane rule), host-computed integrals",
-        "config": workload_config(ds, mol, args.alkane, args.precision, world),
+        "config": dict(workload_config(ds, mol, args.alkane, args.precision, world),
+                       autotune={"chosen": tune["chosen"], "best_ms": tune["best_ms"],
+                                 "candidates": [(c["effective"], round(c["ms"], 4))
+                                                for c in tune["candidates"]]}),
         "e2e": {"value": world * 1e3 / e2e_ms, "unit": "builds/s",
                 "h2d_bytes_per_step": int(Ph.nbytes + Ch.nbytes),
                 "d2h_bytes_per_step": int(2 * n * n * 8), "host_memory": "page-locked"},
@@ -925,7 +934,10 @@ def main():
     if rank == 0 and not args.no_water:
         out["water"] = run_water(dev)
     if rank == 0 and not args.no_cpu_baseline:
-        kc = k_split_plan(nbf, naux, nocc)[1]
+        # the oracle sums the exchange in the k parts the FP64 device build
+        # used (the autotuner's choice, or the built-in plan)
+        kc = eng.get_tunables()["fp64_kchunk"] if fp64 is not None else \
+            k_split_plan(nbf, naux, nocc)[1]
         tcpu, Jo, Ko = cpu_reference_build(ds, Cocc, P, kc, want=True)
         if fp64 is not None and args.kmethod == "dfmo":
             # the FP64 device path against the CPU oracle on the same inputs

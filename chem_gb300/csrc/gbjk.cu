@@ -84,6 +84,10 @@ struct gbjk_ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int overlap_sms = kDefaultOverlapSms;
+  // launch configuration: requested (0 = built-in rule) and in effect
+  gbjk_tunables tune{};
+  gbjk_tunables tune_eff{};
+  long long kchunk = 0;  // FP64 exchange k per part
   std::string err;
   int64_t launches = 0;
   size_t dev_bytes = 0;
@@ -269,6 +273,48 @@ void add_tiles(std::vector<GemmTile>& tiles, int group, int M, int N, int k0, in
 constexpr int kNarrowN = 16;
 constexpr long long kElemOutputs = 1 << 20;
 
+// FP64 launch choices for a problem (the built-in rules where req asks for
+// none): tile width of the half transform and fit (1 = one thread per
+// output), exchange tile (1 or 64) and the exchange's k parts.
+struct Fp64Plan {
+  bool elem_ht, narrow, elem_k;
+  int ht_tn, ks;
+  long long kc;
+};
+gbjk_status fp64_plan(int nbf, int naux, int nocc, const gbjk_tunables& req, Fp64Plan* pl) {
+  if (nbf <= 0 || naux <= 0 || nocc <= 0) return GBJK_INVALID_ARG;
+  const int t = req.fp64_ht_tn;
+  if (t != 0 && t != 1 && t != 16 && t != 32 && t != 64) return GBJK_INVALID_ARG;
+  if (req.fp64_k_tile != 0 && req.fp64_k_tile != 1 && req.fp64_k_tile != 64)
+    return GBJK_INVALID_ARG;
+  if (req.fp64_kchunk < 0) return GBJK_INVALID_ARG;
+  if (t == 0) {
+    pl->elem_ht = (long long)nbf * naux * nocc <= kElemOutputs;
+    pl->narrow = !pl->elem_ht && nocc <= kNarrowN;
+    // occupied widths just above a multiple of 32 (e.g. 81) pad less with
+    // 64 x 32 tiles than with 64 x 64 ones
+    const bool mid = !pl->elem_ht && !pl->narrow && cdiv(nocc, 32) * 32 < cdiv(nocc, 64) * 64;
+    pl->ht_tn = pl->elem_ht || pl->narrow ? 16 : (mid ? 32 : 64);
+  } else {
+    pl->elem_ht = t == 1;
+    pl->narrow = t == 16;
+    pl->ht_tn = t == 1 ? 16 : t;
+  }
+  const long long kdim = (long long)naux * nocc;
+  int ks = 1;
+  long long kc = kdim;
+  gbjk_k_split_plan(nbf, naux, nocc, &ks, &kc);
+  if (req.fp64_kchunk > 0) {
+    kc = std::min((req.fp64_kchunk + 15) / 16 * 16, (kdim + 15) / 16 * 16);
+    ks = (int)((kdim + kc - 1) / kc);
+  }
+  pl->ks = ks;
+  pl->kc = kc;
+  pl->elem_k = req.fp64_k_tile == 0 ? (long long)nbf * nbf * ks <= kElemOutputs
+                                    : req.fp64_k_tile == 1;
+  return GBJK_OK;
+}
+
 // Coefficient workspaces shared by both paths.
 gbjk_status ensure_c_workspace(gbjk_ctx* ctx, int nocc) {
   if (ctx->wc_nocc == nocc) return GBJK_OK;
@@ -297,23 +343,24 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
   if ((s = ensure_c_workspace(ctx, nocc))) return s;
   if ((s = dalloc(ctx, &ctx->d_H, hsz))) return s;
   if ((s = dalloc(ctx, &ctx->d_H2, hsz))) return s;
-  // split-K of the exchange GEMM: enough tiles to fill the GPU
+  // split-K of the exchange GEMM and tile shapes: requested or by rule
   const long long kdim = (long long)naux * nocc;
-  int ks = 1;
-  long long kchunk64 = kdim;
-  gbjk_k_split_plan(ctx->nbf, ctx->naux, nocc, &ks, &kchunk64);
+  Fp64Plan pl;
+  if ((s = fp64_plan(ctx->nbf, ctx->naux, nocc, ctx->tune, &pl)))
+    return fail(ctx, s, "invalid FP64 tunables");
+  const int ks = pl.ks;
+  const long long kchunk64 = pl.kc;
   ctx->ksplit = ks;
+  ctx->kchunk = kchunk64;
   if ((s = dalloc(ctx, &ctx->d_Kpart, (size_t)ks * nbf * nbf))) return s;
-  const bool elem_ht = (long long)nbf * naux * nocc <= kElemOutputs;
-  const bool elem_k = (long long)nbf * nbf * ks <= kElemOutputs;
-  const bool narrow = !elem_ht && nocc <= kNarrowN;
-  // occupied widths just above a multiple of 32 (e.g. 81) pad less with
-  // 64 x 32 tiles than with 64 x 64 ones
-  const bool mid = !elem_ht && !narrow && cdiv(nocc, 32) * 32 < cdiv(nocc, 64) * 64;
+  const bool elem_ht = pl.elem_ht, elem_k = pl.elem_k, narrow = pl.narrow;
   ctx->narrow = narrow;
-  ctx->ht_tn = elem_ht || narrow ? 16 : (mid ? 32 : 64);
+  ctx->ht_tn = pl.ht_tn;
   ctx->elem_ht = elem_ht;
   ctx->elem_k = elem_k;
+  ctx->tune_eff.fp64_ht_tn = elem_ht ? 1 : pl.ht_tn;
+  ctx->tune_eff.fp64_k_tile = elem_k ? 1 : 64;
+  ctx->tune_eff.fp64_kchunk = kchunk64;
   const int ht_tm = elem_ht ? 16 : 64, ht_tn = ctx->ht_tn;
   const int k_t = elem_k ? 16 : 64;
 
@@ -953,6 +1000,271 @@ gbjk_status gbjk_set_overlap(gbjk_ctx* ctx, int sms) {
   if (sms < 0 || sms > 128) return fail(ctx, GBJK_INVALID_ARG, "gbjk_set_overlap: 0 <= sms <= 128");
   if (sms != ctx->overlap_sms) ctx->epoch++;  // the launch sequence changes
   ctx->overlap_sms = sms;
+  ctx->tune.overlap_sms = sms;
+  return GBJK_OK;
+}
+
+// --- launch configuration and autotuning -----------------------------------
+static gbjk_status check_ready(gbjk_ctx* ctx);
+
+gbjk_status gbjk_tune_plan(int nbf, int naux, int nocc, const gbjk_tunables* req,
+                           gbjk_tunables* eff, int* ksplit) {
+  gbjk_tunables r{};
+  if (req) r = *req;
+  Fp64Plan pl;
+  gbjk_status s = fp64_plan(nbf, naux, nocc, r, &pl);
+  if (s) return s;
+  if (eff) {
+    *eff = r;
+    eff->fp64_ht_tn = pl.elem_ht ? 1 : pl.ht_tn;
+    eff->fp64_k_tile = pl.elem_k ? 1 : 64;
+    eff->fp64_kchunk = pl.kc;
+  }
+  if (ksplit) *ksplit = pl.ks;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_set_tunables(gbjk_ctx* ctx, const gbjk_tunables* t) {
+  if (!ctx || !t) return GBJK_INVALID_ARG;
+  if (t->split_ksplit < 0 || t->overlap_sms < 0 || t->overlap_sms > 128)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_set_tunables: split_ksplit or overlap_sms out of range");
+  Fp64Plan pl;
+  if (fp64_plan(ctx->nbf, ctx->naux, 1, *t, &pl))
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_set_tunables: invalid FP64 choice");
+  const gbjk_tunables o = ctx->tune;
+  if (o.fp64_ht_tn != t->fp64_ht_tn || o.fp64_k_tile != t->fp64_k_tile ||
+      o.fp64_kchunk != t->fp64_kchunk)
+    ctx->ws_nocc = -1;  // FP64 plans and workspaces are rebuilt at the next build
+  if (o.split_ksplit != t->split_ksplit) {
+    ctx->split.ks_req = t->split_ksplit;
+    ctx->split.release_build();
+  }
+  ctx->overlap_sms = t->overlap_sms;
+  ctx->tune = *t;
+  ctx->epoch++;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_get_tunables(const gbjk_ctx* ctx, gbjk_tunables* t) {
+  if (!ctx || !t) return GBJK_INVALID_ARG;
+  *t = ctx->tune_eff;
+  t->split_ksplit = ctx->split.ks_eff;
+  t->overlap_sms = ctx->overlap_sms;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_tune_signature(const gbjk_ctx* ctx, int kmethod, int nocc, char* sig,
+                                size_t len) {
+  if (!ctx || !sig || !len) return GBJK_INVALID_ARG;
+  cudaDeviceProp prop{};
+  std::string dev = "unknown";
+  int nsm = 0;
+  if (cudaGetDeviceProperties(&prop, ctx->device) == cudaSuccess) {
+    dev = prop.name;
+    nsm = prop.multiProcessorCount;
+  }
+  for (char& c : dev)
+    if (c == ' ' || c == '|') c = '_';
+  long long ksum = 0;
+  for (int k : ctx->panelK) ksum += k;
+  std::snprintf(sig, len,
+                "gbjk1|%s|sm%d|prec%d|k%d|j%d|fit%d|xb%d|nbf%d|naux%d|nocc%d|nblk%d|nnz%lld|kp%lld",
+                dev.c_str(), nsm, ctx->precision, kmethod, ctx->jmode, ctx->fitted ? 1 : 0,
+                ctx->split.xb_req, ctx->nbf, ctx->naux, nocc, ctx->nblk, ctx->nnz, ksum);
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_tune_cache_lookup(const char* path, const char* sig, gbjk_tunables* t) {
+  if (!path || !sig || !t) return GBJK_INVALID_ARG;
+  FILE* f = std::fopen(path, "r");
+  if (!f) return GBJK_NOT_READY;
+  char line[1024], key[768];
+  bool found = false;
+  gbjk_tunables v{};
+  while (std::fgets(line, sizeof line, f)) {
+    gbjk_tunables x{};
+    if (std::sscanf(line, "%767s %d %d %lld %d %d", key, &x.fp64_ht_tn, &x.fp64_k_tile,
+                    &x.fp64_kchunk, &x.split_ksplit, &x.overlap_sms) == 6 &&
+        std::strcmp(key, sig) == 0) {
+      v = x;  // the last line of a signature wins
+      found = true;
+    }
+  }
+  std::fclose(f);
+  if (!found) return GBJK_NOT_READY;
+  *t = v;
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_tune_cache_store(const char* path, const char* sig, const gbjk_tunables* t) {
+  if (!path || !sig || !t || std::strlen(sig) >= 768 || std::strchr(sig, ' ') ||
+      std::strchr(sig, '\n'))
+    return GBJK_INVALID_ARG;
+  FILE* f = std::fopen(path, "a");
+  if (!f) return GBJK_INVALID_ARG;
+  std::fprintf(f, "%s %d %d %lld %d %d\n", sig, t->fp64_ht_tn, t->fp64_k_tile, t->fp64_kchunk,
+               t->split_ksplit, t->overlap_sms);
+  const bool ok = std::fclose(f) == 0;
+  return ok ? GBJK_OK : GBJK_INVALID_ARG;
+}
+
+namespace {
+std::string tunables_json(const gbjk_tunables& t) {
+  char b[256];
+  std::snprintf(b, sizeof b,
+                "{\"fp64_ht_tn\": %d, \"fp64_k_tile\": %d, \"fp64_kchunk\": %lld, "
+                "\"split_ksplit\": %d, \"overlap_sms\": %d}",
+                t.fp64_ht_tn, t.fp64_k_tile, t.fp64_kchunk, t.split_ksplit, t.overlap_sms);
+  return b;
+}
+
+// Mean time of `reps` builds on the context's own buffers after one
+// warm-up build that prepares the plans; < 0 on failure.
+double time_builds(gbjk_ctx* ctx, int kmethod, int nocc, int reps, gbjk_status* st) {
+  *st = gbjk_compute_jk_dev(ctx, kmethod, ctx->d_P, ctx->d_C, nocc, ctx->d_J, ctx->d_K);
+  if (*st || (*st = gbjk_synchronize(ctx))) return -1.0;
+  cudaEvent_t a = get_event(ctx), b = get_event(ctx);
+  cudaEventRecord(a, ctx->stream);
+  for (int r = 0; r < reps && !*st; ++r)
+    *st = gbjk_compute_jk_dev(ctx, kmethod, ctx->d_P, ctx->d_C, nocc, ctx->d_J, ctx->d_K);
+  cudaEventRecord(b, ctx->stream);
+  if (!*st) *st = gbjk_synchronize(ctx);
+  float ms = -1.f;
+  if (!*st) cudaEventElapsedTime(&ms, a, b);
+  ctx->ev_pool.push_back(a);
+  ctx->ev_pool.push_back(b);
+  return *st ? -1.0 : (double)ms / std::max(1, reps);
+}
+}  // namespace
+
+gbjk_status gbjk_autotune(gbjk_ctx* ctx, int kmethod, const double* P, const double* C, int nocc,
+                          int reps, const char* cache_path, char* report, size_t report_len) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (!P || !C || nocc <= 0 || reps < 0)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_autotune: density, coefficients and nocc needed");
+  if (kmethod != GBJK_K_DFMO && kmethod != GBJK_K_DFLMO)
+    return fail(ctx, GBJK_INVALID_ARG, "Invalid kmethod");
+  auto put = [&](const std::string& r) {
+    if (report && report_len) std::snprintf(report, report_len, "%s", r.c_str());
+  };
+  char sig[768];
+  gbjk_tune_signature(ctx, kmethod, nocc, sig, sizeof sig);
+  gbjk_tunables cached{};
+  if (cache_path && gbjk_tune_cache_lookup(cache_path, sig, &cached) == GBJK_OK) {
+    if ((s = gbjk_set_tunables(ctx, &cached))) return s;
+    put(std::string("{\"signature\": \"") + sig + "\", \"source\": \"cache\", \"chosen\": " +
+        tunables_json(cached) + "}");
+    return GBJK_OK;
+  }
+  if (reps == 0) return fail(ctx, GBJK_NOT_READY, "gbjk_autotune: signature not in the cache");
+  if ((s = ensure_j_workspace(ctx)) || (s = ensure_c_workspace(ctx, nocc))) return s;
+  const size_t n2 = (size_t)ctx->nbf * ctx->nbf;
+  CK(cudaMemcpyAsync(ctx->d_P, P, n2 * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(ctx->d_C, C, (size_t)ctx->nbf * nocc * sizeof(double),
+                     cudaMemcpyHostToDevice, ctx->stream));
+  const bool prof = ctx->profile;
+  ctx->profile = false;
+  ctx->split.profile = false;
+  // the choices of the other precision stay; this precision's start from
+  // the built-in rules
+  const bool fp64 = ctx->precision == GBJK_FP64;
+  gbjk_tunables cur = ctx->tune;
+  if (fp64) {
+    cur.fp64_ht_tn = cur.fp64_k_tile = 0;
+    cur.fp64_kchunk = 0;
+  } else {
+    cur.split_ksplit = cur.overlap_sms = 0;
+  }
+  if ((s = gbjk_set_tunables(ctx, &cur))) return s;
+  std::string cands;
+  int ncand = 0;
+  auto measure = [&](const gbjk_tunables& t, double* ms) -> gbjk_status {
+    gbjk_status st = gbjk_set_tunables(ctx, &t);
+    if (st) return st;
+    *ms = time_builds(ctx, kmethod, nocc, reps, &st);
+    if (st) return st;
+    gbjk_tunables eff{};
+    gbjk_get_tunables(ctx, &eff);
+    char b[64];
+    std::snprintf(b, sizeof b, ", \"ms\": %.5f}", *ms);
+    cands += (ncand++ ? ", " : "") + std::string("{\"requested\": ") + tunables_json(t) +
+             ", \"effective\": " + tunables_json(eff) + b;
+    return GBJK_OK;
+  };
+  double best = 0.0;
+  s = measure(cur, &best);
+  gbjk_tunables base{};
+  gbjk_get_tunables(ctx, &base);  // what the rules chose
+  const long long big = 2 * kElemOutputs;  // one thread per output beyond: far too slow
+  // one dimension at a time, each starting from the best so far
+  std::vector<std::vector<gbjk_tunables>> dims;
+  if (fp64) {
+    std::vector<gbjk_tunables> d1, d2, d3;
+    for (int tn : {1, 16, 32, 64}) {
+      if (tn == 1 && (long long)ctx->nbf * ctx->naux * nocc > big) continue;
+      gbjk_tunables t{};
+      t.fp64_ht_tn = tn;
+      d1.push_back(t);
+    }
+    for (int kt : {1, 64}) {
+      if (kt == 1 && (long long)ctx->nbf * ctx->nbf * ctx->ksplit > big) continue;
+      gbjk_tunables t{};
+      t.fp64_k_tile = kt;
+      d2.push_back(t);
+    }
+    for (long long mul : {1LL, 2LL, 4LL}) {  // chunk x 1/2, 1, 2
+      gbjk_tunables t{};
+      t.fp64_kchunk = std::max(16LL, base.fp64_kchunk * mul / 2);
+      d3.push_back(t);
+    }
+    dims = {d1, d2, d3};
+  } else {
+    std::vector<gbjk_tunables> d1, d2;
+    for (int mul : {1, 2, 4}) {  // parts x 1/2, 1, 2
+      gbjk_tunables t{};
+      t.split_ksplit = std::max(1, base.split_ksplit * mul / 2);
+      d1.push_back(t);
+    }
+    for (int o : {0, 8, 16}) {
+      gbjk_tunables t{};
+      t.overlap_sms = o;
+      d2.push_back(t);
+    }
+    dims = {d1, d2};
+  }
+  for (size_t d = 0; d < dims.size() && !s; ++d) {
+    gbjk_tunables pick = cur;
+    for (const gbjk_tunables& c : dims[d]) {
+      gbjk_tunables t = cur;
+      if (fp64) {
+        if (d == 0) t.fp64_ht_tn = c.fp64_ht_tn;
+        if (d == 1) t.fp64_k_tile = c.fp64_k_tile;
+        if (d == 2) t.fp64_kchunk = c.fp64_kchunk;
+      } else {
+        if (d == 0) t.split_ksplit = c.split_ksplit;
+        if (d == 1) t.overlap_sms = c.overlap_sms;
+      }
+      double ms = 0.0;
+      if ((s = measure(t, &ms))) break;
+      if (ms < best) {
+        best = ms;
+        pick = t;
+      }
+    }
+    cur = pick;
+  }
+  ctx->profile = prof;
+  ctx->split.profile = prof;
+  if (s) return s;
+  if ((s = gbjk_set_tunables(ctx, &cur))) return s;
+  if (cache_path && gbjk_tune_cache_store(cache_path, sig, &cur) != GBJK_OK)
+    return fail(ctx, GBJK_INVALID_ARG, std::string("gbjk_autotune: cannot write ") + cache_path);
+  char b[64];
+  std::snprintf(b, sizeof b, ", \"best_ms\": %.5f", best);
+  put(std::string("{\"signature\": \"") + sig + "\", \"source\": \"timed\", \"reps\": " +
+      std::to_string(reps) + ", \"chosen\": " + tunables_json(cur) + b +
+      ", \"candidates\": [" + cands + "]}");
   return GBJK_OK;
 }
 

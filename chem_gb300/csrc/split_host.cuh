@@ -72,6 +72,8 @@ struct SplitState {
   // the exchange GEMM leaves free (0: all SMs)
   cudaEvent_t ev_ht = nullptr;
   int k_grid = 0;
+  // requested exchange k parts (0 = choose_ksplit) and the number in effect
+  int ks_req = 0, ks_eff = 0;
   double ms[4] = {0, 0, 0, 0};
   int64_t nl[4] = {0, 0, 0, 0};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -390,6 +392,12 @@ struct SplitState {
   };
   std::vector<BatchPlan> plans;
 
+  // parts of the exchange's k range: requested, or by the wave model below;
+  // never fewer than an item's int64 headroom allows (<= 8192 k per item)
+  int exchange_ksplit(int nkt_total, int ntile) const {
+    if (ks_req > 0) return std::max(cdiv_(nkt_total, 256), std::min(ks_req, nkt_total));
+    return choose_ksplit(nkt_total, ntile);
+  }
   int choose_ksplit(int nkt_total, int ntile) const {
     const int ks_min = cdiv_(nkt_total, 256);  // int64 headroom: <= 8192 k per item
     double best = 1e300;
@@ -437,7 +445,7 @@ struct SplitState {
     if (xlast != xb) sizes.push_back(xlast);
     ksplit = 1;
     for (int xbc : sizes)
-      ksplit = std::max(ksplit, choose_ksplit(cdiv_((long long)pad32(xbc) * hld, kTileK), ntile));
+      ksplit = std::max(ksplit, exchange_ksplit(cdiv_((long long)pad32(xbc) * hld, kTileK), ntile));
     if (alloc(&d_Cslices, (size_t)ctot) != cudaSuccess ||
         alloc(&d_eC, (size_t)nblk * c_nrb * 32) != cudaSuccess ||
         alloc(&d_H, (size_t)nbf * hk) != cudaSuccess ||
@@ -502,7 +510,7 @@ struct SplitState {
       pl.nht = (int)items.size() - pl.ht0;
       // exchange: upper tiles, split over k
       const int nk_b = cdiv_((long long)pad32(xbc) * hld, kTileK);
-      const int ksb = choose_ksplit(nk_b, ntile);
+      const int ksb = exchange_ksplit(nk_b, ntile);
       const int kt_per = cdiv_(nk_b, ksb);
       pl.ksplit = cdiv_(nk_b, kt_per);
       pl.k0 = (int)items.size();
@@ -556,6 +564,7 @@ struct SplitState {
       plans.push_back(pl);
     }
     ht_nitems = plans[0].nht;
+    ks_eff = plans[0].ksplit;
     k_nitems = plans[0].nk;
     c_maxthreads = 0;
     c_maxrows = std::max(nocc_, maxb);

@@ -35,6 +35,14 @@ class GbjkShells(C.Structure):
                 ("alpha", C.POINTER(C.c_double)), ("coef", C.POINTER(C.c_double))]
 
 
+class GbjkTunables(C.Structure):
+    _fields_ = [("fp64_ht_tn", C.c_int), ("fp64_k_tile", C.c_int), ("fp64_kchunk", C.c_longlong),
+                ("split_ksplit", C.c_int), ("overlap_sms", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class GbjkDesc(C.Structure):
     _fields_ = [("nbf", C.c_int), ("naux", C.c_int), ("nblk", C.c_int),
                 ("blk_size", C.POINTER(C.c_int)), ("panel_K", C.POINTER(C.c_int)),
@@ -97,6 +105,15 @@ def lib():
         L.gbjk_kernel_launches.restype = C.c_int64
         L.gbjk_k_split_plan.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int),
                                          C.POINTER(C.c_longlong)]
+        tp = C.POINTER(GbjkTunables)
+        L.gbjk_tune_plan.argtypes = [C.c_int, C.c_int, C.c_int, tp, tp, C.POINTER(C.c_int)]
+        L.gbjk_set_tunables.argtypes = [vp, tp]
+        L.gbjk_get_tunables.argtypes = [vp, tp]
+        L.gbjk_tune_signature.argtypes = [vp, C.c_int, C.c_int, C.c_char_p, C.c_size_t]
+        L.gbjk_tune_cache_lookup.argtypes = [C.c_char_p, C.c_char_p, tp]
+        L.gbjk_tune_cache_store.argtypes = [C.c_char_p, C.c_char_p, tp]
+        L.gbjk_autotune.argtypes = [vp, C.c_int, dp, dp, C.c_int, C.c_int, C.c_char_p,
+                                    C.c_char_p, C.c_size_t]
         L.gbjk_profile.argtypes = [vp, C.c_int]
         L.gbjk_profile_read.argtypes = [vp, C.c_int, C.POINTER(C.c_char_p), dp,
                                         C.POINTER(C.c_int64)]
@@ -112,6 +129,28 @@ def lib():
 
 def _dp(a):
     return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def tune_plan(nbf, naux, nocc, **req):
+    """Effective FP64 launch choices (dict) and the exchange's number of k
+    parts for a problem and requested tunables (gbjk_tune_plan; no GPU)."""
+    r = GbjkTunables(**req)
+    e = GbjkTunables()
+    ks = C.c_int()
+    if lib().gbjk_tune_plan(nbf, naux, nocc, C.byref(r), C.byref(e), C.byref(ks)) != 0:
+        raise RuntimeError("gbjk_tune_plan: invalid arguments")
+    return e.as_dict(), ks.value
+
+
+def tune_cache_lookup(path, sig):
+    t = GbjkTunables()
+    rc = lib().gbjk_tune_cache_lookup(path.encode(), sig.encode(), C.byref(t))
+    return t.as_dict() if rc == 0 else None
+
+
+def tune_cache_store(path, sig, **tun):
+    if lib().gbjk_tune_cache_store(path.encode(), sig.encode(), C.byref(GbjkTunables(**tun))):
+        raise RuntimeError("gbjk_tune_cache_store failed")
 
 
 def k_split_plan(nbf, naux, nocc):
@@ -213,6 +252,37 @@ class JKEngine:
         B = np.empty(self.layout.nnz)
         self._check(lib().gbjk_download_b(self.h, _dp(B)), "gbjk_download_b")
         return B
+
+    def set_tunables(self, **tun):
+        """Launch choices (gbjk_tunables fields; omitted or 0 = built-in rule)."""
+        self._check(lib().gbjk_set_tunables(self.h, C.byref(GbjkTunables(**tun))),
+                    "gbjk_set_tunables")
+
+    def get_tunables(self):
+        """The launch choices in effect at the last build."""
+        t = GbjkTunables()
+        self._check(lib().gbjk_get_tunables(self.h, C.byref(t)), "gbjk_get_tunables")
+        return t.as_dict()
+
+    def tune_signature(self, kmethod="dfmo", nocc=None):
+        buf = C.create_string_buffer(768)
+        self._check(lib().gbjk_tune_signature(self.h, KMETHODS[kmethod], int(nocc), buf, 768),
+                    "gbjk_tune_signature")
+        return buf.value.decode()
+
+    def autotune(self, Ptot, Cocc, kmethod="dfmo", reps=3, cache=None):
+        """Time candidate launch configurations of one Fock build at the
+        engine's precision and keep the fastest (gbjk_autotune); with a
+        cache file holding this problem's signature the recorded choice is
+        adopted without timing.  Returns the report as a dict."""
+        import json
+        P = np.ascontiguousarray(Ptot, dtype=np.float64)
+        Cm = np.ascontiguousarray(Cocc, dtype=np.float64)
+        buf = C.create_string_buffer(1 << 16)
+        self._check(lib().gbjk_autotune(self.h, KMETHODS[kmethod], _dp(P), _dp(Cm), Cm.shape[1],
+                                        int(reps), cache.encode() if cache else None, buf,
+                                        1 << 16), "gbjk_autotune")
+        return json.loads(buf.value.decode())
 
     def set_overlap(self, sms):
         """SMs the mixed-path exchange leaves to the concurrent J column

@@ -209,6 +209,61 @@ void* gbjk_stream(gbjk_ctx* ctx);
  * No counterpart in the reference (DBCSR does not specify its order). */
 gbjk_status gbjk_k_split_plan(int nbf, int naux, int nocc, int* ksplit, long long* kchunk);
 
+/* ---- Launch configuration and autotuning ----------------------------------
+ * The choices a Fock build's launches depend on.  0 in a field selects the
+ * engine's built-in rule for it.
+ *   fp64_ht_tn    FP64 half transform and fit: 1 (one thread per output,
+ *                 16 x 16 tiles), 16, 32 or 64 (64-row tiles of that width)
+ *   fp64_k_tile   FP64 exchange: 1 (one thread per output) or 64
+ *   fp64_kchunk   FP64 exchange: k per split-K part (rounded up to a
+ *                 multiple of 16; the parts are summed in order)
+ *   split_ksplit  split-precision exchange: parts of the k range (at least
+ *                 the number an item's int64 headroom needs)
+ *   overlap_sms   as gbjk_set_overlap
+ * Every FP64 choice keeps each output an in-order fma chain over its k
+ * part, so FP64 results depend on fp64_kchunk only, which
+ * gbjk_tune_plan publishes for a checker.  No counterpart in the reference,
+ * whose small-block GEMMs are DBCSR's (src/dbcsrx/dbcsr_tensor_ops.hpp:
+ * 128-137). */
+typedef struct gbjk_tunables {
+  int fp64_ht_tn;
+  int fp64_k_tile;
+  long long fp64_kchunk;
+  int split_ksplit;
+  int overlap_sms;
+} gbjk_tunables;
+
+/* Effective FP64 choices for a problem size and requested tunables (the
+ * built-in rules filled in, fp64_kchunk rounded and clamped); *ksplit is
+ * the number of exchange parts.  Needs no GPU. */
+gbjk_status gbjk_tune_plan(int nbf, int naux, int nocc, const gbjk_tunables* req,
+                           gbjk_tunables* eff, int* ksplit);
+/* Requested tunables of a context (takes effect at its next build). */
+gbjk_status gbjk_set_tunables(gbjk_ctx* ctx, const gbjk_tunables* t);
+/* The values in effect at the context's last build (requested or rule). */
+gbjk_status gbjk_get_tunables(const gbjk_ctx* ctx, gbjk_tunables* t);
+/* Problem signature of the context for precision, kmethod and nocc (the
+ * autotuning cache key): writes at most len bytes into sig. */
+gbjk_status gbjk_tune_signature(const gbjk_ctx* ctx, int kmethod, int nocc, char* sig,
+                                size_t len);
+/* Tuning cache: a text file, one line per tuned signature,
+ *   <signature> <fp64_ht_tn> <fp64_k_tile> <fp64_kchunk> <split_ksplit> <overlap_sms>
+ * the last line of a signature wins.  Lookup returns GBJK_NOT_READY when
+ * the file or the signature is missing.  Need no GPU. */
+gbjk_status gbjk_tune_cache_lookup(const char* path, const char* sig, gbjk_tunables* t);
+gbjk_status gbjk_tune_cache_store(const char* path, const char* sig, const gbjk_tunables* t);
+/* Autotune one Fock build (host P_tot and C_occ, the same arguments as
+ * gbjk_compute_jk) at the context's precision.  With a cache_path whose
+ * file holds this signature the recorded choice is adopted without
+ * timing.  Otherwise candidates are timed one dimension at a time (each
+ * with one warm-up build and `reps` timed builds, CUDA events on the
+ * context's stream), the fastest is kept, and it is appended to the cache
+ * when cache_path is given.  A JSON report of the candidates and times goes
+ * to report (at most report_len bytes, may be NULL). */
+gbjk_status gbjk_autotune(gbjk_ctx* ctx, int kmethod, const double* Ptot, const double* Cocc,
+                          int nocc, int reps, const char* cache_path, char* report,
+                          size_t report_len);
+
 /* ---- SOS-AO-MP2 Laplace batch ------------------------------------------
  * Replaces the Z builder of megalochem's Laplace loop: mp::LL_FULL_Z
  * (src/mp/z_full.cpp:427-620, "mi, Xmn -> Xin", "Na, XiN -> Xia", then
