@@ -995,6 +995,16 @@ gbjk_status gbjk_download_b(gbjk_ctx* ctx, double* B) {
   return GBJK_OK;
 }
 
+gbjk_status gbjk_test_split_stall(gbjk_ctx* ctx, int item, double wait_ms) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (item >= 0 && !(wait_ms >= 1.0 && wait_ms <= 2000.0))
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_test_split_stall: 1 <= wait_ms <= 2000");
+  ctx->split.stop_item = item < 0 ? -1 : item;
+  ctx->split.spin_ns = item < 0 ? kSpinNs : (unsigned long long)(wait_ms * 1e6);
+  ctx->epoch++;  // kernel arguments of a captured build change
+  return GBJK_OK;
+}
+
 gbjk_status gbjk_set_overlap(gbjk_ctx* ctx, int sms) {
   if (!ctx) return GBJK_INVALID_ARG;
   if (sms < 0 || sms > 128) return fail(ctx, GBJK_INVALID_ARG, "gbjk_set_overlap: 0 <= sms <= 128");
@@ -1617,6 +1627,8 @@ gbjk_status gbjk_compute_k_ao_dev(gbjk_ctx* ctx, const double* dP, double* dK) {
   if (ctx->precision == GBJK_SPLIT_BF16 && !ctx->split.b_ready &&
       (s = ctx->split.prepare_b(ctx->stream, ctx->d_B, ctx->d_Linv, &ctx->launches, &ctx->err)))
     return s;
+  if (ctx->precision == GBJK_SPLIT_BF16 && (s = ctx->split.clear_error(ctx->stream)))
+    return fail(ctx, s, "split path: memset failed");
   if ((s = ctx->aok.prepare(ctx->stream, ctx->precision, L, ctx->d_B,
                             ctx->fitted ? nullptr : ctx->d_Vinv, ctx->split, &ctx->launches,
                             &ctx->err)))
@@ -1669,6 +1681,8 @@ gbjk_status gbjk_compute_k_lmo_asym(gbjk_ctx* ctx, const double* U, const double
     for (int n = 0; n < nbf; ++n) v[(size_t)n * nocc + i] = Vt[(size_t)i * nbf + n];
   CK(cudaMemcpyAsync(a.d_U, U, (size_t)nbf * nocc * 8, cudaMemcpyHostToDevice, ctx->stream));
   CK(cudaMemcpyAsync(a.d_V, v.data(), v.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->precision == GBJK_SPLIT_BF16 && (s = ctx->split.clear_error(ctx->stream)))
+    return fail(ctx, s, "split path: memset failed");
   {
     PhaseScope ps(ctx, PH_KGEMM);
     if ((s = a.run(ctx->stream, nbf, ctx->naux, ctx->nblk, ctx->ncols_total, ctx->d_colmap,
@@ -1713,6 +1727,7 @@ gbjk_status gbjk_mp2_compute_dev(gbjk_ctx* ctx) {
   if ((s = check_ready(ctx))) return s;
   if (!ctx->mp2.ready || ctx->mp2.precision != ctx->precision)
     return fail(ctx, GBJK_NOT_READY, "gbjk_mp2_compute_dev: set the factors first (after any precision change)");
+  if ((s = ctx->split.clear_error(ctx->stream))) return fail(ctx, s, "split path: memset failed");
   return ctx->mp2.run(ctx->stream, ctx->nbf, ctx->naux, ctx->nblk, ctx->ncols_total,
                       ctx->d_colmap, ctx->split, &ctx->launches, &ctx->err);
 }

@@ -34,8 +34,10 @@
 // a chunk end, then the approximate pairs (15 pairs as 9 MMAs of N = 96 or
 // 192); at a chunk start it issues the approximate pairs first, so the drain
 // of chunk c overlaps the approximate MMAs of two k-tiles.  Every wait is
-// bounded (kSpinNs); on timeout the CTA records an error code, drains its
-// own copies and MMAs and frees TMEM.
+// bounded (spin_ns, kSpinNs by default); on timeout the CTA records an error
+// code, every other wait of the launch gives up, and before exiting each CTA
+// waits (bounded by time only) for its own bulk copies, on the stages' full
+// barriers, and its own MMAs, on a commit barrier, then frees TMEM.
 //
 // Shared-memory operand layout: K-major, no swizzle, 8x8 core matrices
 // (128 B); within a tile of R rows x 32 k the element (r, k) sits at byte
@@ -140,21 +142,33 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
-// Bounded wait; on timeout records `code` in *err and returns false.  The
-// error flag and the timer are read every 1024 polls only, so a completed
-// phase is seen within one try_wait.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code) {
+// Bounded wait; on timeout records `code` in *err and returns false, and
+// it gives up as soon as another wait of the launch has recorded an error.
+// The error flag and the timer are read every 1024 polls only, so a
+// completed phase is seen within one try_wait.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int* err, int code,
+                                          unsigned long long spin_ns) {
   if (mbar_try_wait(bar, parity)) return true;
   const unsigned long long t0 = globaltimer();
   for (uint32_t i = 1;; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     if ((i & 1023) == 0) {
       if (*(volatile int*)err != 0) return false;
-      if (globaltimer() - t0 > kSpinNs) {
+      if (globaltimer() - t0 > spin_ns) {
         atomicCAS(err, 0, code);
         return false;
       }
     }
+  }
+}
+// Wait bounded by time only (not by the error flag): for the completion of
+// this CTA's own bulk copies and MMAs before it exits, which always come.
+__device__ __forceinline__ bool mbar_wait_own(uint64_t* bar, uint32_t parity,
+                                              unsigned long long spin_ns) {
+  const unsigned long long t0 = globaltimer();
+  for (uint32_t i = 0;; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 1023) == 1023 && globaltimer() - t0 > spin_ns) return false;
   }
 }
 __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
@@ -393,7 +407,8 @@ __global__ void k_split_tiles(const SplitJob* __restrict__ jobs) {
 // the accumulator of diagonal d sits at TMEM column d * kTileN.
 
 __global__ void __launch_bounds__(kThreads, 1)
-    k_split_gemm(const SplitItem* __restrict__ items, int nitems, int* __restrict__ err) {
+    k_split_gemm(const SplitItem* __restrict__ items, int nitems, int* __restrict__ err,
+                 int stop_item, unsigned long long spin_ns) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   // 1 KB aligned operand ring, then barriers
   unsigned char* smem =
@@ -401,7 +416,7 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char* sA = smem;                       // kStages * kBytesA
   unsigned char* sB = smem + kStages * kBytesA;   // kStages * kBytesB
   __shared__ uint64_t full_bar[kStages], empty_bar[kStages];
-  __shared__ uint64_t exact_full, exact_empty, final_full, final_empty;
+  __shared__ uint64_t exact_full, exact_empty, final_full, final_empty, mma_drain;
   __shared__ uint32_t tmem_base_sh;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -414,6 +429,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     mbar_init(&exact_empty, kEpiWarps);
     mbar_init(&final_full, 1);
     mbar_init(&final_empty, kEpiWarps);
+    mbar_init(&mma_drain, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -434,12 +450,20 @@ __global__ void __launch_bounds__(kThreads, 1)
       int stage = 0;
       uint32_t phase = 0;
       bool ok = true;
+      // full-barrier parity of the last copies issued into each stage
+      uint32_t last_par[kStages];
+      bool issued[kStages];
+#pragma unroll
+      for (int i = 0; i < kStages; ++i) issued[i] = false;
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+        // test hook: stop producing at work item stop_item, so the
+        // consumers' bounded waits run out (the launch reports a timeout)
+        if (it == stop_item) break;
         const SplitItem w = items[it];
         const uint32_t a_run = (uint32_t)(kTileM / 32) * kImage * 2;
         const uint32_t b_run = (uint32_t)(kTileN / 32) * kImage * 2;
         for (int k = 0; k < w.nkt && ok; ++k) {
-          ok = mbar_wait(&empty_bar[stage], phase ^ 1, err, 1);
+          ok = mbar_wait(&empty_bar[stage], phase ^ 1, err, 1, spin_ns);
           if (!ok) break;
           mbar_arrive_expect_tx(&full_bar[stage], kSlices * (a_run + b_run));
           const long long kt = w.kt0 + k;
@@ -449,22 +473,19 @@ __global__ void __launch_bounds__(kThreads, 1)
             bulk_g2s(sA + stage * kBytesA + s * a_run, ga, a_run, &full_bar[stage]);
             bulk_g2s(sB + stage * kBytesB + s * b_run, gb, b_run, &full_bar[stage]);
           }
+          last_par[stage] = phase;
+          issued[stage] = true;
           if (++stage == kStages) {
             stage = 0;
             phase ^= 1;
           }
         }
       }
-      // wait until every issued copy has landed before the CTA can exit:
-      // the MMA thread consumes stages in order, so waiting for the ring to
-      // drain (each stage's empty barrier) covers all copies in flight
-      for (int i = 0; i < kStages; ++i) {
-        mbar_wait(&empty_bar[stage], phase ^ 1, err, 2);
-        if (++stage == kStages) {
-          stage = 0;
-          phase ^= 1;
-        }
-      }
+      // before the CTA can exit, every copy it issued must have landed,
+      // also after a timeout: wait on the full barrier of each stage's last
+      // copies (bounded by time only; copies always complete)
+      for (int i = 0; i < kStages; ++i)
+        if (issued[i]) mbar_wait_own(&full_bar[i], last_par[i], spin_ns);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer
@@ -480,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int k = 0; k < w.nkt && ok; ++k) {
           const bool chunk_start = (k % kChunkTiles) == 0;
           const bool chunk_end = ((k + 1) % kChunkTiles) == 0 || k + 1 == w.nkt;
-          ok = mbar_wait(&full_bar[stage], phase, err, 5);
+          ok = mbar_wait(&full_bar[stage], phase, err, 5, spin_ns);
           if (!ok) break;
           tc_fence_after();
           const uint64_t adesc = smem_desc(smem_u32(sA + stage * kBytesA));
@@ -518,7 +539,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // drained the previous item's last chunk, which comes before its
             // fold of d = 3, 4; so the exact pairs go first and overlap that
             // fold, and the d = 3, 4 pairs wait for it
-            ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4);
+            ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4, spin_ns);
             ex_phase ^= 1;
             if (!ok) {
               mma_commit(&empty_bar[stage]);  // the ring drain still completes
@@ -526,7 +547,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             issue(0, 4);
             if (chunk_end) mma_commit(&exact_full);
-            ok = mbar_wait(&final_empty, fin_phase ^ 1, err, 3);
+            ok = mbar_wait(&final_empty, fin_phase ^ 1, err, 3, spin_ns);
             fin_phase ^= 1;
             if (!ok) {
               mma_commit(&empty_bar[stage]);
@@ -538,7 +559,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             // exact drain does not read them, so they overlap the epilogue's
             // drain of the previous chunk; the exact pairs wait for it
             issue(4, 9);
-            ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4);
+            ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4, spin_ns);
             ex_phase ^= 1;
             if (!ok) {
               mma_commit(&empty_bar[stage]);  // the ring drain still completes
@@ -559,6 +580,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
         if (ok) mma_commit(&final_full);
       }
+      // every MMA this thread issued completes before TMEM is freed and the
+      // CTA exits, also after a timeout (commit tracks all prior MMAs)
+      mma_commit(&mma_drain);
+      mbar_wait_own(&mma_drain, 0, spin_ns);
     }
   } else {
     // ---------------- epilogue (warps 2..13)
@@ -582,7 +607,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (int c = 0; c < kEpiCols; ++c) V[c] = 0;
       const int nchunks = (w.nkt + kChunkTiles - 1) / kChunkTiles;
       for (int ch = 0; ch < nchunks && ok; ++ch) {
-        ok = mbar_wait(&exact_full, ex_phase, err, 6);
+        ok = mbar_wait(&exact_full, ex_phase, err, 6, spin_ns);
         ex_phase ^= 1;
         if (!ok) break;
         tc_fence_after();
@@ -610,7 +635,7 @@ __global__ void __launch_bounds__(kThreads, 1)
         if (lane == 0) mbar_arrive(&exact_empty);
       }
       if (!ok) break;
-      ok = mbar_wait(&final_full, fin_phase, err, 7);
+      ok = mbar_wait(&final_full, fin_phase, err, 7, spin_ns);
       fin_phase ^= 1;
       if (!ok) break;
       tc_fence_after();

@@ -74,6 +74,10 @@ struct SplitState {
   int k_grid = 0;
   // requested exchange k parts (0 = choose_ksplit) and the number in effect
   int ks_req = 0, ks_eff = 0;
+  // test hook (gbjk_test_split_stall): the producer stops at this work item
+  // of every split GEMM launch (-1: never), and the waits' time limit
+  int stop_item = -1;
+  unsigned long long spin_ns = kSpinNs;
   double ms[4] = {0, 0, 0, 0};
   int64_t nl[4] = {0, 0, 0, 0};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
@@ -208,7 +212,7 @@ struct SplitState {
       attr_set = true;
     }
     const int grid = std::min(n, std::max(1, nsm - leave_sms));
-    k_split_gemm<<<grid, kThreads, kSmemBytes, st>>>(items, n, d_err);
+    k_split_gemm<<<grid, kThreads, kSmemBytes, st>>>(items, n, d_err, stop_item, spin_ns);
     (*launches)++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -637,6 +641,11 @@ struct SplitState {
   // --- per build ------------------------------------------------------------
   gbjk_status run_k(cudaStream_t st, double* dK, int64_t* launches, std::string* err) {
     gbjk_status s;
+    // the flag a timed-out wait sets is per build: cleared at its start
+    if (cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) {
+      *err = "split path: memset failed";
+      return GBJK_CUDA_ERROR;
+    }
     {
       Scope sc(this, 2, st);
       k_row_maxexp<<<dim3(cdiv_((long long)c_maxrows * 32, 256), 2 * nblk), 256, 0, st>>>(d_jobs);
@@ -699,6 +708,11 @@ struct SplitState {
     return GBJK_OK;
   }
 
+  // clear the timed-out-wait flag at the start of a computation (stream order)
+  gbjk_status clear_error(cudaStream_t st) {
+    if (d_err && cudaMemsetAsync(d_err, 0, sizeof(int), st) != cudaSuccess) return GBJK_CUDA_ERROR;
+    return GBJK_OK;
+  }
   // error code recorded by a timed-out wait inside the split GEMM (0 = none)
   int read_error() {
     int h = 0;

@@ -72,6 +72,7 @@ def lib():
         L.gbjk_set_precision.argtypes = [vp, C.c_int, C.c_int]
         L.gbjk_set_jmode.argtypes = [vp, C.c_int]
         L.gbjk_set_overlap.argtypes = [vp, C.c_int]
+        L.gbjk_test_split_stall.argtypes = [vp, C.c_int, C.c_double]
         L.gbjk_get_overlap.argtypes = [vp]
         L.gbjk_get_overlap.restype = C.c_int
         L.gbjk_set_fitted.argtypes = [vp, C.c_int]
@@ -283,6 +284,13 @@ class JKEngine:
                                         int(reps), cache.encode() if cache else None, buf,
                                         1 << 16), "gbjk_autotune")
         return json.loads(buf.value.decode())
+
+    def test_split_stall(self, item, wait_ms=5.0):
+        """Failure-detection test hook (gbjk_test_split_stall): item >= 0
+        makes the split GEMM stop producing at that work item, so the
+        bounded waits run out and builds report TIMEOUT; -1 restores."""
+        self._check(lib().gbjk_test_split_stall(self.h, int(item), float(wait_ms)),
+                    "gbjk_test_split_stall")
 
     def set_overlap(self, sms):
         """SMs the mixed-path exchange leaves to the concurrent J column
@@ -587,6 +595,14 @@ def create_k(engine: JKEngine, method="dfmo") -> K:
         return DFMO_K(engine)
     if method == "dflmo":
         return DFLMO_K(engine)
-    if method == "dfao":
+    if method in ("dfao", "dfmem"):
+        # fock::DFMEM_K (src/fock/jkdf.cpp:650-859) forms the same exchange
+        # as DFAO_K with the fit on the other factor:
+        #   K = -sum_{X,s} (X|ns) [V^-1 (X|mr) P_rs]  =  -(B^T V^-1 B P)
+        # so both names select the DF-AO builder
         return DFAO_K(engine)
+    if method == "dfrobust":
+        # fock::DFROBUST_K needs the PARI metric; with the Coulomb metric
+        # the reference refuses it (src/fock/jkbuilder.hpp:598-603)
+        raise RuntimeError("Cannot use robust k for method other than PARI")
     raise RuntimeError("Invalid kmethod")

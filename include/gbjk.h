@@ -135,6 +135,14 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
                                 const int* pair_J, const unsigned char* keep, const int* col_IJ,
                                 const int* col_JI);
 
+/* Test hook for failure detection: item >= 0 makes every split-precision
+ * GEMM launch of the context stop issuing operand copies at work item
+ * `item`, with each pipeline wait bounded by wait_ms (1..2000) instead of
+ * 2 s.  The waiting threads give up, every CTA waits for its own copies
+ * and MMAs, and the build reports GBJK_TIMEOUT; the context stays usable.
+ * item < 0 restores normal operation.  No counterpart in the reference. */
+gbjk_status gbjk_test_split_stall(gbjk_ctx* ctx, int item, double wait_ms);
+
 /* Mixed-precision build: after the half transform the J column sums
  * (HBM-bound) run on a second stream of the context beside the exchange
  * GEMM (tensor-bound), which then leaves `sms` SMs to them; 0 runs the

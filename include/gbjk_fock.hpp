@@ -213,7 +213,13 @@ inline std::shared_ptr<J> create_j(std::shared_ptr<engine> e, const std::string&
 inline std::shared_ptr<K> create_k(std::shared_ptr<engine> e, const std::string& method) {
   if (method == "dfmo") return std::make_shared<DF_K>(std::move(e), GBJK_K_DFMO);
   if (method == "dflmo") return std::make_shared<DF_K>(std::move(e), GBJK_K_DFLMO);
-  if (method == "dfao") return std::make_shared<DFAO_K>(std::move(e));
+  // fock::DFMEM_K (src/fock/jkdf.cpp:650-859) is the DF-AO exchange with the
+  // fit on the other factor, -(B^T V^-1 B P): the same builder serves it
+  if (method == "dfao" || method == "dfmem") return std::make_shared<DFAO_K>(std::move(e));
+  // fock::DFROBUST_K needs the PARI metric, which the reference requires
+  // (src/fock/jkbuilder.hpp:598-603); this engine has the Coulomb metric only
+  if (method == "dfrobust")
+    throw std::runtime_error("Cannot use robust k for method other than PARI");
   throw std::runtime_error("Invalid kmethod");
 }
 
