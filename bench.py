@@ -880,6 +880,23 @@ def main():
         r_mix, t_mix = run("split", "cholesky", "cholesky")
         r_mixv, t_mixv = run("split", "cholesky", "vinv")
         r_pure, t_pure = run("split", "cholesky")
+        # the same mixed SCF with each iteration's device work in CUDA graphs
+        from chem_gb300.scf import run_rhf_device
+        eng.set_precision("split")
+        eng.set_jmode("cholesky")
+        run_rhf_device(eng, ds.S, ds.Hcore, mol.nuclear_repulsion(), mol.nocc, kmethod=args.kmethod,
+                       conv=1e-8, max_iter=3)  # captures the graphs
+        t0 = time.perf_counter()
+        r_dev = run_rhf_device(eng, ds.S, ds.Hcore, mol.nuclear_repulsion(), mol.nocc,
+                               kmethod=args.kmethod, conv=1e-8)
+        t_dev = time.perf_counter() - t0
+        eng.set_precision("split")
+        eng.set_jmode("cholesky")
+        t0 = time.perf_counter()
+        r_devsw = run_rhf_device(eng, ds.S, ds.Hcore, mol.nuclear_repulsion(), mol.nocc,
+                                 kmethod=args.kmethod, conv=1e-8,
+                                 switch=fp64_switch(eng, "cholesky"))
+        t_devsw = time.perf_counter() - t0
         r_aud, _ = run("split", "cholesky", audit=audit)
         r_ref6, t_ref6 = run("fp64", "vinv", max_vecs=6)
         ec = {"fp64_vinv_route": e_exact_metric(r_ref),
@@ -894,6 +911,12 @@ def main():
                "mixed_then_fp64_cholesky": rec(r_mix, t_mix, switch=sw_note + ", Cholesky route"),
                "mixed_then_fp64_vinv": rec(r_mixv, t_mixv, switch=sw_note + ", V^-1 route"),
                "mixed_only": rec(r_pure, t_pure),
+               "mixed_only_device_graphs": rec(r_dev, t_dev, note="P = C C^T, Fock build, "
+                                               "F = H + J + K, energy, FPS - SPF, RMS and DIIS "
+                                               "overlaps in one CUDA graph; DIIS combination "
+                                               "and X F X in a second; FP64 eigh on the host"),
+               "mixed_then_fp64_cholesky_device_graphs": rec(r_devsw, t_devsw),
+               "dE_mixed_only_device_vs_fp64_cholesky": r_dev.energy - r_chol.energy,
                "dE_mixed_only_vs_fp64_cholesky": r_pure.energy - r_chol.energy,
                "dE_mixed_then_fp64_cholesky_vs_fp64_cholesky": r_mix.energy - r_chol.energy,
                "dE_mixed_then_fp64_vinv_vs_fp64_vinv": r_mixv.energy - r_ref.energy,

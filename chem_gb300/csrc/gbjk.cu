@@ -28,6 +28,7 @@
 #include "asymk_host.cuh"
 #include "kernels_fp64.cuh"
 #include "mp2_host.cuh"
+#include "scf_host.cuh"
 #include "split_host.cuh"
 
 using namespace gbjk;
@@ -138,6 +139,8 @@ struct gbjk_ctx {
   AoKState aok;
   // non-symmetric DF-LMO exchange (left and right coefficients)
   AsymKState asymk;
+  // SCF iteration on the device (graphs around the Fock build)
+  ScfState scf;
   // profiling
   bool profile = false;
   cudaEvent_t ev[PH_COUNT][2] = {};
@@ -728,6 +731,7 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   ctx->mp2.release();
   ctx->aok.release();
   ctx->asymk.release();
+  ctx->scf.release();
   ctx->split.release();
   void* ptrs[] = {ctx->d_blk_of, ctx->d_boff,  ctx->d_panelK, ctx->d_cmoff, ctx->d_colmap,
                   ctx->d_panel_off, ctx->d_pg_off, ctx->d_B, ctx->d_Linv, ctx->d_Vinv,
@@ -1560,7 +1564,7 @@ gbjk_status gbjk_compute_k(gbjk_ctx* ctx, int kmethod, const double* Cocc, int n
 }
 
 size_t gbjk_device_bytes(const gbjk_ctx* ctx) {
-  return ctx ? ctx->dev_bytes + ctx->split.bytes + ctx->mp2.bytes + ctx->aok.bytes +
+  return ctx ? ctx->dev_bytes + ctx->split.bytes + ctx->mp2.bytes + ctx->aok.bytes + ctx->scf.bytes +
                    ctx->asymk.bytes
              : 0;
 }
@@ -1692,6 +1696,122 @@ gbjk_status gbjk_compute_k_lmo_asym(gbjk_ctx* ctx, const double* U, const double
   if ((s = filter(ctx, ctx->d_K))) return s;
   CK(cudaMemcpyAsync(K, ctx->d_K, (size_t)nbf * nbf * 8, cudaMemcpyDeviceToHost, ctx->stream));
   return gbjk_synchronize(ctx);
+}
+
+// --- SCF iteration on the device -------------------------------------------
+
+gbjk_status gbjk_scf_begin(gbjk_ctx* ctx, const double* H, const double* S, const double* X,
+                           int nocc, int max_diis) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  if (!H || !S || !X || nocc <= 0 || nocc > ctx->nbf || max_diis < 1 || max_diis > kScfMaxDiis)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_scf_begin: H, S, X, 0 < nocc <= nbf, 1 <= max_diis <= 16");
+  return (s = ctx->scf.begin(ctx->stream, ctx->nbf, nocc, max_diis, H, S, X, &ctx->err))
+             ? fail(ctx, s, ctx->err)
+             : GBJK_OK;
+}
+
+gbjk_status gbjk_scf_build(gbjk_ctx* ctx, int kmethod, const double* Cocc, int slot, double* out) {
+  gbjk_status s;
+  if ((s = check_ready(ctx))) return s;
+  ScfState& sc = ctx->scf;
+  if (!sc.ready) return fail(ctx, GBJK_NOT_READY, "gbjk_scf_build: call gbjk_scf_begin first");
+  if (!Cocc || !out || slot < 0 || slot >= sc.nslots)
+    return fail(ctx, GBJK_INVALID_ARG, "gbjk_scf_build: coefficients, output and 0 <= slot < max_diis");
+  if (kmethod != GBJK_K_DFMO && kmethod != GBJK_K_DFLMO)
+    return fail(ctx, GBJK_INVALID_ARG, "Invalid kmethod");
+  CK(cudaMemcpyAsync(sc.dC, Cocc, (size_t)sc.nbf * sc.nocc * sizeof(double),
+                     cudaMemcpyHostToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(sc.dslot, &slot, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  const bool stale = !sc.gA || sc.epA != build_epoch(ctx) || sc.kmethodA != kmethod;
+  if (!stale && !ctx->profile) {
+    CK(cudaGraphLaunch(sc.gA, ctx->stream));
+    ctx->launches += sc.launchesA;
+  } else {
+    // direct launches (they prepare every plan and buffer of the build) ...
+    ctx->launches += sc.launch_pre(ctx->stream);
+    CK(cudaGetLastError());
+    if ((s = gbjk_compute_jk_dev(ctx, kmethod, sc.dPt, sc.dC, sc.nocc, sc.dJ, sc.dK))) return s;
+    ctx->launches += sc.launch_post(ctx->stream);
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpyAsync(out, sc.dscal, (size_t)(2 + sc.nslots) * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  if ((s = gbjk_synchronize(ctx))) return s;
+  if (stale && !ctx->profile) {
+    // ... then the same sequence is recorded for the next iterations
+    if (sc.gA) cudaGraphExecDestroy(sc.gA);
+    if (sc.grA) cudaGraphDestroy(sc.grA);
+    sc.gA = nullptr;
+    sc.grA = nullptr;
+    const uint64_t ep = build_epoch(ctx);
+    if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const int64_t l0 = ctx->launches;
+      int64_t n = sc.launch_pre(ctx->stream);
+      gbjk_status cs = gbjk_compute_jk_dev(ctx, kmethod, sc.dPt, sc.dC, sc.nocc, sc.dJ, sc.dK);
+      n += sc.launch_post(ctx->stream) + (ctx->launches - l0);
+      ctx->launches = l0;
+      cudaGraph_t g = nullptr;
+      const cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+      if (!cs && e == cudaSuccess && build_epoch(ctx) == ep &&
+          cudaGraphInstantiate(&sc.gA, g, 0) == cudaSuccess) {
+        sc.grA = g;
+        sc.epA = ep;
+        sc.kmethodA = kmethod;
+        sc.launchesA = n;
+      } else if (g) {
+        cudaGraphDestroy(g);
+      }
+    }
+    cudaGetLastError();  // a build that cannot be captured keeps direct launches
+  }
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_scf_extrapolate(gbjk_ctx* ctx, const double* coef, double* Fo) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  ScfState& sc = ctx->scf;
+  if (!sc.ready) return fail(ctx, GBJK_NOT_READY, "gbjk_scf_extrapolate: call gbjk_scf_begin first");
+  if (!coef || !Fo) return fail(ctx, GBJK_INVALID_ARG, "gbjk_scf_extrapolate: null argument");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaMemcpyAsync(sc.dcoef, coef, (size_t)sc.nslots * sizeof(double), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  if (!sc.gB) {
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    sc.launchesB = sc.launch_extrapolate(ctx->stream);
+    CK(cudaStreamEndCapture(ctx->stream, &g));
+    CK(cudaGraphInstantiate(&sc.gB, g, 0));
+    sc.grB = g;
+  }
+  CK(cudaGraphLaunch(sc.gB, ctx->stream));
+  ctx->launches += sc.launchesB;
+  CK(cudaMemcpyAsync(Fo, sc.dFo, (size_t)sc.nbf * sc.nbf * sizeof(double),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  return gbjk_synchronize(ctx);
+}
+
+gbjk_status gbjk_scf_read(gbjk_ctx* ctx, int slot, double* F, double* J, double* K) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  ScfState& sc = ctx->scf;
+  if (!sc.ready) return fail(ctx, GBJK_NOT_READY, "gbjk_scf_read: call gbjk_scf_begin first");
+  if (slot < 0 || slot >= sc.nslots) return fail(ctx, GBJK_INVALID_ARG, "gbjk_scf_read: slot");
+  CK(cudaSetDevice(ctx->device));
+  const size_t n2 = (size_t)sc.nbf * sc.nbf;
+  if (F)
+    CK(cudaMemcpyAsync(F, sc.dFring + (size_t)slot * n2, n2 * 8, cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  if (J) CK(cudaMemcpyAsync(J, sc.dJ, n2 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  if (K) CK(cudaMemcpyAsync(K, sc.dK, n2 * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  return gbjk_synchronize(ctx);
+}
+
+gbjk_status gbjk_scf_end(gbjk_ctx* ctx) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->scf.release();
+  return GBJK_OK;
 }
 
 // --- SOS-AO-MP2 Laplace batch -----------------------------------------------

@@ -73,6 +73,11 @@ def lib():
         L.gbjk_set_jmode.argtypes = [vp, C.c_int]
         L.gbjk_set_overlap.argtypes = [vp, C.c_int]
         L.gbjk_test_split_stall.argtypes = [vp, C.c_int, C.c_double]
+        L.gbjk_scf_begin.argtypes = [vp, dp, dp, dp, C.c_int, C.c_int]
+        L.gbjk_scf_build.argtypes = [vp, C.c_int, dp, C.c_int, dp]
+        L.gbjk_scf_extrapolate.argtypes = [vp, dp, dp]
+        L.gbjk_scf_read.argtypes = [vp, C.c_int, dp, dp, dp]
+        L.gbjk_scf_end.argtypes = [vp]
         L.gbjk_get_overlap.argtypes = [vp]
         L.gbjk_get_overlap.restype = C.c_int
         L.gbjk_set_fitted.argtypes = [vp, C.c_int]
@@ -284,6 +289,44 @@ class JKEngine:
                                         int(reps), cache.encode() if cache else None, buf,
                                         1 << 16), "gbjk_autotune")
         return json.loads(buf.value.decode())
+
+    # --- SCF iteration on the device (gbjk_scf_*) ---------------------------
+    def scf_begin(self, H, S, X, nocc, max_diis=8):
+        """Upload H, S and the symmetric orthogonaliser X for the device SCF
+        iteration; max_diis ring slots for Fock and error matrices."""
+        self._scf_nslots = int(max_diis)
+        a = [np.ascontiguousarray(m, dtype=np.float64) for m in (H, S, X)]
+        self._check(lib().gbjk_scf_begin(self.h, _dp(a[0]), _dp(a[1]), _dp(a[2]), int(nocc),
+                                         int(max_diis)), "gbjk_scf_begin")
+
+    def scf_build(self, Cocc, slot, kmethod="dfmo"):
+        """One SCF build on the device from C_occ: returns (E_el, rms,
+        overlaps of the new error matrix with every ring slot)."""
+        Cm = np.ascontiguousarray(Cocc, dtype=np.float64)
+        out = np.empty(2 + self._scf_nslots)
+        self._check(lib().gbjk_scf_build(self.h, KMETHODS[kmethod], _dp(Cm), int(slot), _dp(out)),
+                    "gbjk_scf_build")
+        return float(out[0]), float(out[1]), out[2:].copy()
+
+    def scf_extrapolate(self, coef):
+        """Fo = X (sum_j coef[j] F_j) X from the ring (device)."""
+        c = np.zeros(self._scf_nslots)
+        c[:len(coef)] = coef
+        Fo = np.empty((self.nbf, self.nbf))
+        self._check(lib().gbjk_scf_extrapolate(self.h, _dp(c), _dp(Fo)), "gbjk_scf_extrapolate")
+        return Fo
+
+    def scf_read(self, slot, jk=False):
+        """F of a ring slot (and J, K of the last build when jk)."""
+        F = np.empty((self.nbf, self.nbf))
+        J = np.empty_like(F) if jk else None
+        K = np.empty_like(F) if jk else None
+        self._check(lib().gbjk_scf_read(self.h, int(slot), _dp(F), _dp(J) if jk else None,
+                                        _dp(K) if jk else None), "gbjk_scf_read")
+        return (F, J, K) if jk else F
+
+    def scf_end(self):
+        self._check(lib().gbjk_scf_end(self.h), "gbjk_scf_end")
 
     def test_split_stall(self, item, wait_ms=5.0):
         """Failure-detection test hook (gbjk_test_split_stall): item >= 0

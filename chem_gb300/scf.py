@@ -123,3 +123,76 @@ def run_rhf(S, Hcore, enuc, nocc, jk, conv=1e-8, max_iter=100, diis_start=0, max
         else:
             F = F_new
     return SCFResult(E, False, max_iter, Cm, e, P, F_new, hist, audits)
+
+
+def run_rhf_device(engine, S, Hcore, enuc, nocc, kmethod="dfmo", conv=1e-8, max_iter=100,
+                   max_vecs=8, switch=None, switch_thresh=1e-5, log=None, audit=None):
+    """The same SCF as run_rhf with each iteration's device work in CUDA
+    graphs (JKEngine.scf_*): P = C C^T, the Fock build, F = H + J + K, the
+    energy, the error matrix FPS - SPF with its RMS and the DIIS overlaps
+    run on the GPU (one graph), and the DIIS combination with X F X (a
+    second graph).  The host solves the DIIS system and diagonalises in
+    FP64, as megalochem does (src/hf/hfscf.cpp:386-459).  DIIS keeps the
+    last max_vecs (F, error) pairs in device ring slots.
+    audit(P_alpha, C_occ, J, K) -> dict is called on every build (it
+    downloads J and K)."""
+    s, U = np.linalg.eigh(S)
+    X = U @ np.diag(s ** -0.5) @ U.T
+    engine.scf_begin(Hcore, S, X, nocc, max_vecs)
+    Bm = np.zeros((max_vecs, max_vecs))
+    order = []  # ring slots in use, oldest first
+    nxt = 0
+    Fo = X.T @ Hcore @ X
+    E_old = 0.0
+    hist, audits = [], []
+    switched = switch is None
+    try:
+        for it in range(max_iter):
+            e, Cp = np.linalg.eigh(Fo)
+            Cm = X @ Cp
+            Cocc = np.ascontiguousarray(Cm[:, :nocc])
+            slot = nxt % max_vecs
+            E_el, rms, ov = engine.scf_build(Cocc, slot, kmethod)
+            E = E_el + enuc
+            if audit is not None:
+                _, J, K = engine.scf_read(slot, jk=True)
+                audits.append(audit(Cocc @ Cocc.T, Cocc, J, K))
+            hist.append((it, E, E - E_old, rms))
+            if log:
+                log(f"iter {it:3d}  E {E:.12f}  dE {E - E_old:.3e}  rms {rms:.3e}")
+            if not switched and rms < switch_thresh:
+                # as run_rhf: the switch iteration's F is used as it is and
+                # not kept for DIIS (its ring slot is reused next)
+                switch()
+                switched = True
+                E_old = E
+                c = np.zeros(max_vecs)
+                c[slot] = 1.0
+                Fo = engine.scf_extrapolate(c)
+                continue
+            if it > 0 and rms < conv and switched:
+                F = engine.scf_read(slot)
+                return SCFResult(E, True, it + 1, Cm, e, Cocc @ Cocc.T, F, hist, audits)
+            E_old = E
+            nxt += 1
+            if slot in order:
+                order.remove(slot)
+            order.append(slot)
+            Bm[slot, :] = ov
+            Bm[:, slot] = ov
+            c = np.zeros(max_vecs)
+            if len(order) < 2:
+                c[slot] = 1.0
+            else:
+                n = len(order)
+                Bs = -np.ones((n + 1, n + 1))
+                Bs[n, n] = 0.0
+                Bs[:n, :n] = Bm[np.ix_(order, order)]
+                rhs = np.zeros(n + 1)
+                rhs[n] = -1.0
+                c[order] = np.linalg.lstsq(Bs, rhs, rcond=None)[0][:n]
+            Fo = engine.scf_extrapolate(c)
+        F = engine.scf_read(slot)
+        return SCFResult(E, False, max_iter, Cm, e, Cocc @ Cocc.T, F, hist, audits)
+    finally:
+        engine.scf_end()

@@ -217,6 +217,34 @@ void* gbjk_stream(gbjk_ctx* ctx);
  * No counterpart in the reference (DBCSR does not specify its order). */
 gbjk_status gbjk_k_split_plan(int nbf, int naux, int nocc, int* ksplit, long long* kchunk);
 
+/* ---- SCF iteration on the device -----------------------------------------
+ * The loop body of megalochem's closed-shell SCF (hf::hfmod::compute,
+ * src/hf/hfscf.cpp:386-459) around this context's Fock build, as CUDA
+ * graphs on the context's stream; the host keeps the DIIS solve and the
+ * FP64 diagonalisation.
+ * gbjk_scf_begin: core Hamiltonian H, overlap S and a symmetric
+ *   orthogonaliser X (e.g. S^-1/2), host nbf x nbf; nocc; DIIS depth
+ *   max_diis (1..16 ring slots for Fock and error matrices).
+ * gbjk_scf_build: from the occupied coefficients Cocc (host nbf x nocc),
+ *   P_tot = 2 C C^T, the J/K build (kmethod as gbjk_compute_jk),
+ *   F = H + J + K (form_fock, :228-276), E_el = sum P (H + F) (:278-296),
+ *   e = F P S - S P F (:298-324) and its RMS; F and e go into ring slot
+ *   `slot`; out[0] = E_el, out[1] = RMS, out[2 + j] = <e, e_j> for every
+ *   slot j (the DIIS B-matrix row, src/math/solvers/diis.hpp:43-234).  The
+ *   first call (and any after the engine's buffers or settings change)
+ *   launches directly, then records the sequence as a graph for the next.
+ * gbjk_scf_extrapolate: Fbar = sum_j coef[j] F_j (coef: max_diis values,
+ *   0 for unused slots) and Fo = X Fbar X into host nbf x nbf.
+ * gbjk_scf_read: F of a slot and J, K of the last build to host (any NULL).
+ * gbjk_scf_end: frees the SCF buffers. */
+gbjk_status gbjk_scf_begin(gbjk_ctx* ctx, const double* H, const double* S, const double* X,
+                           int nocc, int max_diis);
+gbjk_status gbjk_scf_build(gbjk_ctx* ctx, int kmethod, const double* Cocc, int slot,
+                           double* out);
+gbjk_status gbjk_scf_extrapolate(gbjk_ctx* ctx, const double* coef, double* Fo);
+gbjk_status gbjk_scf_read(gbjk_ctx* ctx, int slot, double* F, double* J, double* K);
+gbjk_status gbjk_scf_end(gbjk_ctx* ctx);
+
 /* ---- Launch configuration and autotuning ----------------------------------
  * The choices a Fock build's launches depend on.  0 in a field selects the
  * engine's built-in rule for it.
