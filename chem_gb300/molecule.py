@@ -150,7 +150,57 @@ class Molecule:
         return e
 
 
+def rcm_order(coords_bohr, cutoff=5.0):
+    """megalochem's atom reordering (math::rcm, src/math/other/rcm.hpp,
+    applied by default in src/megalochem_driver.cpp:380-399 with a 5 bohr
+    cutoff): atoms closer than `cutoff` are connected; each breadth-first
+    sweep starts from one atom of the most distant pair that still has an
+    atom outside the order (the one with fewer neighbours, or the one not
+    yet placed), neighbours are queued by decreasing degree (ties keep the
+    index order, as the reference's sort does for fewer than 17 neighbours),
+    and the final order is reversed.  Returns the new atom order: atom i of
+    the reordered molecule is atom order[i] of the input."""
+    X = np.asarray(coords_bohr, float)
+    n = len(X)
+    d = np.sqrt(((X[:, None, :] - X[None, :, :]) ** 2).sum(-1))
+    con = d < cutoff
+    deg = con.sum(1) - 1
+    iu = np.triu_indices(n, 1)
+    placed = np.zeros(n, bool)
+    R = []
+
+    def neighbours(p):
+        nb = [i for i in range(n) if con[p, i] and i != p]
+        return sorted(nb, key=lambda i: -deg[i])  # stable: ties keep index order
+
+    while len(R) < n:
+        free = ~(placed[iu[0]] & placed[iu[1]])
+        dv = np.where(free, d[iu], 0.0)
+        k = int(np.argmax(dv))  # first pair of the row-major scan at the maximum
+        n1, n2 = int(iu[0][k]), int(iu[1][k])
+        p = n2 if ((deg[n1] > deg[n2] or placed[n1]) and not placed[n2]) else n1
+        R.append(p)
+        placed[p] = True
+        queue = list(neighbours(p))
+        while queue:
+            q = queue.pop(0)
+            if placed[q]:
+                continue
+            R.append(q)
+            placed[q] = True
+            queue.extend(neighbours(q))
+    return R[::-1]
+
+
 def molecule_from_angstrom(symbols, coords_ang, basis="cc-pvdz", dfbasis="cc-pvdz-jkfit",
-                           charge=0) -> Molecule:
-    return Molecule(list(symbols), np.asarray(coords_ang, float) * BOHR_PER_ANGSTROM,
-                    basis, dfbasis, charge)
+                           charge=0, reorder=False) -> Molecule:
+    """reorder=True applies megalochem's default atom reordering (rcm_order)
+    so that atom blocks, and so J and K element by element, come in the
+    reference's order; the generators here emit chain order."""
+    sym = list(symbols)
+    X = np.asarray(coords_ang, float) * BOHR_PER_ANGSTROM
+    if reorder:
+        order = rcm_order(X)
+        sym = [sym[i] for i in order]
+        X = X[order]
+    return Molecule(sym, X, basis, dfbasis, charge)
