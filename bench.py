@@ -59,6 +59,8 @@ def parse():
     ap.add_argument("--syn-naux", type=int, default=12000)
     ap.add_argument("--syn-nocc", type=int, default=600)
     ap.add_argument("--syn-batch", type=int, default=1000)
+    ap.add_argument("--syn-fp64-full", action="store_true",
+                    help="also one FP64 build at full size (minutes) for split vs FP64")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--rate", type=float, default=20.0)
     ap.add_argument("--budget-gb", type=float, default=150.0)
@@ -378,6 +380,27 @@ def run_synthetic(args):
     eng.synchronize()
     prof = {k: v[0] for k, v in eng.profile_read().items() if v[1]}
     eng.close()
+    full64 = None
+    if args.syn_fp64_full:
+        # the same tensor regenerated for an FP64 engine (auxiliary batches)
+        e64 = JKEngine(layout, None, None, None, fitted=True, synthetic=(20261203, decay),
+                       precision="fp64", aux_batch=args.syn_batch)
+        s64 = torch.cuda.ExternalStream(e64.stream, device=torch.device("cuda", 0))
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        f0.record(s64)
+        e64.compute_jk_dev(0, dC.data_ptr(), nocc, 0, dK.data_ptr())
+        f1.record(s64)
+        e64.synchronize()
+        t64f = f0.elapsed_time(f1) * 1e-3
+        K64f = dK.cpu().numpy()
+        full64 = {"fp64_gpu_s_per_build": t64f, "speedup_split": t64f / (ms * 1e-3),
+                  "max_abs_dK_split_vs_fp64": float(np.abs(K - K64f).max()),
+                  "max_abs_K": float(np.abs(K64f).max()),
+                  "device_gb_fp64": e64.device_bytes / 1e9,
+                  "note": "one FP64 build, pre-fitted tensor, exchange in auxiliary batches"}
+        e64.close()
+        del K64f
     hbm, bf16, _, src = peaks()
     f_ht = 15 * 2.0 * nocc * layout.nnz
     f_k = 15 * 1.0 * naux * nocc * nbf * (nbf + 1)
@@ -415,6 +438,7 @@ def run_synthetic(args):
                           "peak_bf16": bf16, "peak_source": src},
         "K_symmetric_max_asym": float(np.abs(K - K.T).max()),
         "K_trace": float(np.trace(K)),
+        "full_size_fp64": full64,
         "reduced": {"nbf": rn, "naux": ra, "nocc": ro, "max_abs_dK_split_vs_fp64":
                     float(np.abs(Ks - K64).max()), "max_abs_K": float(np.abs(K64).max()),
                     "fp64_gpu_s": t64, "fp64_bitwise_vs_oracle": bool(np.array_equal(K64, Kr)),

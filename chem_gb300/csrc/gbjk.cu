@@ -85,6 +85,23 @@ struct gbjk_ctx {
   cudaStream_t side = nullptr;
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int overlap_sms = kDefaultOverlapSms;
+  // FP64 K of a pre-fitted tensor in auxiliary batches (gbjk_set_aux_batch):
+  // per batch b the half transform of rows [b*xb, b*xb + xbc) (one group per
+  // AO function mu; groups b*nbf .. b*nbf+nbf-1) and its split-K exchange,
+  // accumulated into K in batch order.  Index 0 of the per-size arrays is a
+  // full batch, 1 the shorter last one.
+  struct Fp64Batch {
+    int nocc = -1, xb = 0, nbatch = 0, xlast = 0;
+    int ks[2] = {1, 1};
+    long long kc[2] = {0, 0};
+    int ht_t0[2] = {0, 0}, ht_nt[2] = {0, 0}, k_t0[2] = {0, 0}, k_nt[2] = {0, 0};
+    bool elem_ht[2] = {false, false}, narrow[2] = {false, false}, elem_k[2] = {false, false};
+    int tn[2] = {64, 64};
+    GemmGroup* d_groups = nullptr;
+    GemmTile* d_tiles = nullptr;
+    double* d_H = nullptr;
+    double* d_Kpart = nullptr;
+  } fb;
   // launch configuration: requested (0 = built-in rule) and in effect
   gbjk_tunables tune{};
   gbjk_tunables tune_eff{};
@@ -478,6 +495,168 @@ gbjk_status ensure_k_workspace(gbjk_ctx* ctx, int nocc) {
   return GBJK_OK;
 }
 
+// Batched FP64 exchange of a pre-fitted tensor: plans and buffers per nocc.
+gbjk_status ensure_k_batched(gbjk_ctx* ctx, int nocc) {
+  auto& fb = ctx->fb;
+  if (fb.nocc == nocc) return GBJK_OK;
+  dfree(ctx, &fb.d_groups);
+  dfree(ctx, &fb.d_tiles);
+  dfree(ctx, &fb.d_H);
+  dfree(ctx, &fb.d_Kpart);
+  fb.nocc = -1;
+  gbjk_status s;
+  if ((s = ensure_c_workspace(ctx, nocc))) return s;
+  const int nbf = ctx->nbf, naux = ctx->naux;
+  fb.xb = std::min(naux, std::max(32, ctx->split.xb_req & ~31));
+  fb.nbatch = cdiv(naux, fb.xb);
+  fb.xlast = naux - (fb.nbatch - 1) * fb.xb;
+  const int sizes[2] = {fb.xb, fb.xlast};
+  std::vector<GemmGroup> groups;
+  std::vector<GemmTile> tiles;
+  // half-transform groups, batch after batch: H_b[mu][y][i] = sum_k
+  // B_I[m][Y0 + y][k] Cg_I[k][i] (rows of one AO function)
+  for (int b = 0; b < fb.nbatch; ++b) {
+    const int Y0 = b * fb.xb, xbc = std::min(fb.xb, naux - Y0);
+    for (int I = 0; I < ctx->nblk; ++I)
+      for (int m = 0; m < ctx->bsize[I]; ++m) {
+        GemmGroup g;
+        const int K = ctx->panelK[I];
+        g.A = ctx->d_B + ctx->panel_off[I] + ((long long)m * naux + Y0) * K;
+        g.B = ctx->d_Cg + (long long)ctx->cmoff[I] * nocc;
+        g.C = nullptr;  // set below once d_H exists
+        g.M = xbc;
+        g.N = nocc;
+        g.K = K;
+        g.lda = K;
+        g.ldb = nocc;
+        g.ldc = nocc;
+        g.flags = 0;
+        groups.push_back(g);
+      }
+  }
+  const int ng_ht = (int)groups.size();
+  long long kpart_max = 1;
+  for (int v = 0; v < 2; ++v) {
+    const int xbc = sizes[v];
+    Fp64Plan pl;
+    if ((s = fp64_plan(nbf, xbc, nocc, ctx->tune, &pl))) return fail(ctx, s, "invalid FP64 tunables");
+    fb.elem_ht[v] = pl.elem_ht;
+    fb.narrow[v] = pl.narrow;
+    fb.tn[v] = pl.ht_tn;
+    fb.elem_k[v] = pl.elem_k;
+    fb.ks[v] = pl.ks;
+    fb.kc[v] = pl.kc;
+    kpart_max = std::max<long long>(kpart_max, pl.ks);
+    const int tm = pl.elem_ht ? 16 : 64;
+    // half-transform tiles of one batch of this size (groups 0..nbf-1
+    // relative to the batch's first group)
+    fb.ht_t0[v] = (int)tiles.size();
+    for (int mu = 0; mu < nbf; ++mu) {
+      const int I = ctx->blk_of[mu];
+      if (ctx->panelK[I] == 0) continue;
+      add_tiles(tiles, mu, xbc, nocc, 0, ctx->panelK[I], 0, false, pl.ht_tn, tm);
+    }
+    fb.ht_nt[v] = (int)tiles.size() - fb.ht_t0[v];
+    // exchange of one batch: K_part = H_b H_b^T, upper tiles, split-K
+    GemmGroup g;
+    g.A = nullptr;
+    g.B = nullptr;
+    g.C = nullptr;
+    g.M = nbf;
+    g.N = nbf;
+    g.K = xbc * nocc;
+    g.lda = xbc * nocc;
+    g.ldb = xbc * nocc;
+    g.ldc = nbf;
+    g.flags = kTransB;
+    groups.push_back(g);  // group ng_ht + v
+    const long long kd = (long long)xbc * nocc;
+    const int kt = pl.elem_k ? 16 : 64;
+    fb.k_t0[v] = (int)tiles.size();
+    for (int k = 0; k < pl.ks; ++k) {
+      const int k0 = (int)(k * pl.kc), k1 = (int)std::min<long long>(kd, (k + 1) * pl.kc);
+      add_tiles(tiles, 0, nbf, nbf, k0, std::max(k0, k1), (long long)k * nbf * nbf, true, kt, kt);
+    }
+    fb.k_nt[v] = (int)tiles.size() - fb.k_t0[v];
+  }
+  if ((s = dalloc(ctx, &fb.d_H, (size_t)nbf * fb.xb * nocc))) return s;
+  if ((s = dalloc(ctx, &fb.d_Kpart, (size_t)kpart_max * nbf * nbf))) return s;
+  for (int b = 0; b < fb.nbatch; ++b) {
+    const int xbc = std::min(fb.xb, naux - b * fb.xb);
+    for (int mu = 0; mu < nbf; ++mu)
+      groups[(size_t)b * nbf + mu].C = fb.d_H + (long long)mu * xbc * nocc;
+  }
+  for (int v = 0; v < 2; ++v) {
+    groups[ng_ht + v].A = fb.d_H;
+    groups[ng_ht + v].B = fb.d_H;
+    groups[ng_ht + v].C = fb.d_Kpart;
+  }
+  if ((s = dalloc(ctx, &fb.d_groups, groups.size()))) return s;
+  if ((s = dalloc(ctx, &fb.d_tiles, tiles.size()))) return s;
+  CK(cudaMemcpy(fb.d_groups, groups.data(), groups.size() * sizeof(GemmGroup),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(fb.d_tiles, tiles.data(), tiles.size() * sizeof(GemmTile),
+                cudaMemcpyHostToDevice));
+  ctx->tune_eff.fp64_ht_tn = fb.elem_ht[0] ? 1 : fb.tn[0];
+  ctx->tune_eff.fp64_k_tile = fb.elem_k[0] ? 1 : 64;
+  ctx->tune_eff.fp64_kchunk = fb.kc[0];
+  fb.nocc = nocc;
+  return GBJK_OK;
+}
+
+gbjk_status filter(gbjk_ctx* ctx, double* M);
+
+gbjk_status run_k_batched(gbjk_ctx* ctx, const double* dC, int nocc, double* dK) {
+  gbjk_status s;
+  if ((s = ensure_k_batched(ctx, nocc))) return s;
+  auto& fb = ctx->fb;
+  const int nbf = ctx->nbf;
+  {
+    PhaseScope ps(ctx, PH_GATHER);
+    const long long total = (long long)ctx->ncols_total * nocc;
+    k_gather_cols<<<cdiv(total, 256), 256, 0, ctx->stream>>>(dC, nocc, ctx->d_colmap,
+                                                             ctx->ncols_total, ctx->d_Cg);
+    CKL(PH_GATHER);
+  }
+  const int ng_ht = fb.nbatch * nbf;
+  for (int b = 0; b < fb.nbatch; ++b) {
+    const int v = (b == fb.nbatch - 1 && fb.xlast != fb.xb) ? 1 : 0;
+    const GemmGroup* g = fb.d_groups + (size_t)b * nbf;
+    const GemmTile* t = fb.d_tiles + fb.ht_t0[v];
+    const int nt = fb.ht_nt[v];
+    if (nt) {
+      PhaseScope ps(ctx, PH_HT);
+      if (fb.elem_ht[v])
+        k_gemm_fp64_elem<false><<<nt, 256, 0, ctx->stream>>>(g, t, 1.0);
+      else if (fb.narrow[v])
+        k_gemm_fp64<false, false, 16><<<nt, 64, 0, ctx->stream>>>(g, t, 1.0);
+      else if (fb.tn[v] == 32)
+        k_gemm_fp64<false, false, 32><<<nt, 128, 0, ctx->stream>>>(g, t, 1.0);
+      else
+        k_gemm_fp64<false><<<nt, 256, 0, ctx->stream>>>(g, t, 1.0);
+      CKL(PH_HT);
+    }
+    {
+      PhaseScope ps(ctx, PH_KGEMM);
+      const GemmGroup* gk = fb.d_groups + ng_ht + v;
+      const GemmTile* tk = fb.d_tiles + fb.k_t0[v];
+      if (fb.elem_k[v])
+        k_gemm_fp64_elem<true><<<fb.k_nt[v], 256, 0, ctx->stream>>>(gk, tk, 1.0);
+      else
+        k_gemm_fp64<true><<<fb.k_nt[v], 256, 0, ctx->stream>>>(gk, tk, 1.0);
+      CKL(PH_KGEMM);
+    }
+    {
+      PhaseScope ps(ctx, PH_KREDUCE);
+      const long long n2 = (long long)nbf * nbf;
+      k_splitk_reduce_acc<<<cdiv(n2, 256), 256, 0, ctx->stream>>>(fb.d_Kpart, fb.ks[v], nbf,
+                                                                  -1.0, 1, b > 0 ? 1 : 0, dK);
+      CKL(PH_KREDUCE);
+    }
+  }
+  return filter(ctx, dK);
+}
+
 gbjk_status ensure_j_workspace(gbjk_ctx* ctx) {
   gbjk_status s;
   const size_t nbf = ctx->nbf, naux = ctx->naux;
@@ -741,6 +920,9 @@ void gbjk_destroy(gbjk_ctx* ctx) {
                   ctx->d_groups, ctx->d_tiles};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  for (void* p : {(void*)ctx->fb.d_groups, (void*)ctx->fb.d_tiles, (void*)ctx->fb.d_H,
+                  (void*)ctx->fb.d_Kpart})
+    if (p) cudaFree(p);
   for (auto& pe : ctx->pending) {
     cudaEventDestroy(pe.second.first);
     cudaEventDestroy(pe.second.second);
@@ -769,6 +951,7 @@ gbjk_status gbjk_upload_b(gbjk_ctx* ctx, const double* B) {
   ctx->aok.release();
   ctx->asymk.release();
   ctx->split.invalidate_b();
+  ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
   return GBJK_OK;
 }
 
@@ -786,6 +969,7 @@ gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* 
   ctx->aok.release();
   ctx->asymk.release();
   ctx->split.invalidate_b();
+  ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
   return GBJK_OK;
 }
 
@@ -810,6 +994,7 @@ gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
   ctx->aok.release();
   ctx->asymk.release();
   ctx->split.invalidate_b();
+  ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
   ctx->ws_nocc = -1;  // exchange plan reads H or the fitted H
   return GBJK_OK;
 }
@@ -822,6 +1007,7 @@ gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows) {
   ctx->aok.release();
   ctx->asymk.release();
   ctx->split.invalidate_b();
+  ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
   return GBJK_OK;
 }
 
@@ -844,6 +1030,7 @@ gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, doub
   ctx->aok.release();
   ctx->asymk.release();
   ctx->split.invalidate_b();
+  ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
   return GBJK_OK;
 }
 
@@ -989,6 +1176,7 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
   ctx->aok.release();
   ctx->asymk.release();
   ctx->split.invalidate_b();
+  ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
   return GBJK_OK;
 }
 
@@ -1049,6 +1237,9 @@ gbjk_status gbjk_set_tunables(gbjk_ctx* ctx, const gbjk_tunables* t) {
   if (o.fp64_ht_tn != t->fp64_ht_tn || o.fp64_k_tile != t->fp64_k_tile ||
       o.fp64_kchunk != t->fp64_kchunk)
     ctx->ws_nocc = -1;  // FP64 plans and workspaces are rebuilt at the next build
+  if (o.fp64_ht_tn != t->fp64_ht_tn || o.fp64_k_tile != t->fp64_k_tile ||
+      o.fp64_kchunk != t->fp64_kchunk)
+    ctx->fb.nocc = -1;
   if (o.split_ksplit != t->split_ksplit) {
     ctx->split.ks_req = t->split_ksplit;
     ctx->split.release_build();
@@ -1302,6 +1493,11 @@ static gbjk_status check_ready(gbjk_ctx* ctx) {
   return GBJK_OK;
 }
 
+// FP64 exchange of a pre-fitted tensor with an auxiliary batch size set
+static bool fp64_batched(const gbjk_ctx* ctx) {
+  return ctx->fitted && ctx->split.xb_req > 0 && ctx->split.xb_req < ctx->naux;
+}
+
 static gbjk_status prepare_split(gbjk_ctx* ctx, int nocc) {
   if (ctx->precision != GBJK_SPLIT_BF16) return GBJK_OK;
   return ctx->split.prepare(ctx->stream, ctx->d_B, ctx->d_Linv, ctx->d_Cg, ctx->d_Pg,
@@ -1395,9 +1591,10 @@ gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, co
       if ((s = prepare_split(ctx, nocc))) return s;
       return run_jk_split(ctx, dP, dC, nocc, dJ, dK);
     }
-    if ((s = ensure_k_workspace(ctx, nocc))) return s;
+    if (!fp64_batched(ctx) && (s = ensure_k_workspace(ctx, nocc))) return s;
   }
   if (dJ && (s = run_j(ctx, dP, dJ))) return s;
+  if (dK && fp64_batched(ctx)) return run_k_batched(ctx, dC, nocc, dK);
   if (dK && (s = run_k(ctx, kmethod, dC, nocc, dK))) return s;
   return GBJK_OK;
 }

@@ -281,6 +281,47 @@ int oracle_dfmo_k(const oracle_layout* L, const double* B, const double* Linv, c
   return 0;
 }
 
+/* DF-MO K of a pre-fitted tensor with the auxiliary index in batches of xb
+ * rows (the last batch shorter), as the device's batched FP64 path sums it:
+ * batch b covers t in [X0*nocc, (X0+xbc)*nocc); within it the chunks of
+ * kc_full (kc_last for a shorter last batch) are in-order fma sums added in
+ * order to 0.0; the batch total is negated and added to K (K = -S_0 for the
+ * first batch, then K = -S_b + K). */
+int oracle_dfmo_k_batched(const oracle_layout* L, const double* B, const double* Cm, int nocc,
+                          double* K, double eps, int xb, long long kc_full, long long kc_last) {
+  const int n = L->nbf, naux = L->naux;
+  const long long len = (long long)naux * nocc;
+  if (xb <= 0 || kc_full <= 0 || kc_last <= 0) return 1;
+  double* H = (double*)malloc(sizeof(double) * (size_t)n * len);
+  if (!H) return 2;
+  oracle_half_transform(L, B, Cm, nocc, H);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int mu = 0; mu < n; ++mu)
+    for (int nu = mu; nu < n; ++nu) {
+      const double* a = H + (size_t)mu * len;
+      const double* b = H + (size_t)nu * len;
+      double k = 0.0;
+      for (int X0 = 0; X0 < naux; X0 += xb) {
+        const int xbc = X0 + xb < naux ? xb : naux - X0;
+        const long long kc = xbc == xb ? kc_full : kc_last;
+        const long long u0 = (long long)X0 * nocc, u1 = (long long)(X0 + xbc) * nocc;
+        double s = 0.0;
+        for (long long t0 = u0; t0 < u1; t0 += kc) {
+          const long long t1 = t0 + kc < u1 ? t0 + kc : u1;
+          double p = 0.0;
+          for (long long t = t0; t < t1; ++t) p = fma(a[t], b[t], p);
+          s += p;
+        }
+        k = X0 == 0 ? -s : -s + k;
+      }
+      K[(size_t)mu * n + nu] = k;
+      K[(size_t)nu * n + mu] = k;
+    }
+  oracle_filter(L, K, eps);
+  free(H);
+  return 0;
+}
+
 /* DF-LMO K (symmetric): HT = B C, HTfit = V^-1 HT, K_nm = -sum HT_m HTfit_n
  * (jkdf.cpp:1026-1088). */
 int oracle_dflmo_k(const oracle_layout* L, const double* B, const double* Vinv, const double* Cm,

@@ -52,6 +52,8 @@ def lib():
         L.oracle_df_j.argtypes = [lp, dp, dp, dp, dp, C.c_double]
         L.oracle_df_j_chol.argtypes = [lp, dp, dp, dp, dp, C.c_double]
         L.oracle_dfmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
+        L.oracle_dfmo_k_batched.argtypes = [lp, dp, dp, C.c_int, dp, C.c_double, C.c_int,
+                                            C.c_longlong, C.c_longlong]
         L.oracle_dflmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
         L.oracle_dfao_k.argtypes = [lp, dp, dp, dp, dp, C.c_double, C.c_longlong]
         L.oracle_half_transform.argtypes = [lp, dp, dp, C.c_int, dp]
@@ -115,6 +117,17 @@ class Oracle:
                                  _dp(Cocc), Cocc.shape[1], _dp(K), eps, int(kchunk))
         if rc:
             raise MemoryError("oracle_dfmo_k")
+        return K
+
+    def dfmo_k_batched(self, Cocc, xb, kc_full, kc_last, eps=0.0):
+        """DF-MO K of a pre-fitted tensor summed in auxiliary batches of xb
+        rows (the device's batched FP64 order)."""
+        C_ = np.ascontiguousarray(Cocc, float)
+        K = np.empty((self.layout.nbf, self.layout.nbf))
+        rc = lib().oracle_dfmo_k_batched(C.byref(self.L), _dp(self.B), _dp(C_), C_.shape[1],
+                                         _dp(K), eps, int(xb), int(kc_full), int(kc_last))
+        if rc:
+            raise RuntimeError(f"oracle_dfmo_k_batched failed ({rc})")
         return K
 
     def dflmo_k(self, Vinv, Cocc, eps=0.0, kchunk=0):
