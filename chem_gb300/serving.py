@@ -21,8 +21,11 @@ workspaces) and serves requests as they arrive:
   that is neither resident nor being admitted; so the requests of a
   resident molecule are served together before it is evicted;
 * execution — GPU slots are host threads, each issuing builds on its own
-  engine's CUDA stream, so builds of different molecules overlap on the
-  device; a molecule's builds are serialised on its engine.
+  engine's CUDA stream; a molecule's builds are serialised on its engine.
+  Builds of different molecules are in flight together, but the split
+  GEMMs of a large molecule take every SM (one CTA per SM, 216 KB of shared
+  memory), so they run one after another; the streams overlap only the
+  small kernels, copies and host work around them.
 Every build runs the same deterministic kernels whatever else is in flight,
 so a result in the mix is bit-identical to the same request served alone.
 
