@@ -238,12 +238,15 @@ struct AoKState {
       ptot += (long long)p_nrb * sp.nkt[I] * kSlices * kImage;
     }
     r_nrb = std::max(cdiv_(nbf, kTileM) * (kTileM / 32), cdiv_(nbf, kTileN) * (kTileN / 32));
+    // exchange tiles: a staircase over the upper triangle (column tiles of
+    // row tile r0 start at r0), fewer than on the grid
+    std::vector<std::pair<int, int>> ktiles;
+    for (int r0 = 0; r0 < nbf; r0 += kTileM)
+      for (int c0 = r0; c0 < nbf; c0 += kTileN) ktiles.push_back({r0, c0});
+    for (const auto& t : ktiles) r_nrb = std::max(r_nrb, cdiv_(t.second + kTileN, 32));
+    const int ntile = (int)ktiles.size();
     r_nkt = cdiv_(kdim, kTileK);
     const long long rdig = (long long)r_nrb * r_nkt * kSlices * kImage;
-    int ntile = 0;
-    for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
-      for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt)
-        if ((nt + 1) * kTileN > mt * kTileM) ++ntile;
     const int ks = sp.choose_ksplit(r_nkt, ntile);
     const int kt_per = cdiv_(r_nkt, ks);
     ksplit = cdiv_(r_nkt, kt_per);
@@ -350,25 +353,23 @@ struct AoKState {
     i_k0 = (int)items.size();
     for (int k = 0; k < ksplit; ++k) {
       const int kt0 = k * kt_per, n_kt = std::min(kt_per, r_nkt - kt0);
-      for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
-        for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt) {
-          if ((nt + 1) * kTileN <= mt * kTileM) continue;
+      for (const auto& t : ktiles) {
+          const int r0 = t.first, c0 = t.second;
           SplitItem w = base();
           w.a = d_Cbdig;
           w.a_nrb = r_nrb;
-          w.a_rb0 = mt * (kTileM / 32);
+          w.a_rb0 = r0 / 32;
           w.b = d_Bdig;
           w.b_nrb = r_nrb;
-          w.b_rb0 = nt * (kTileN / 32);
+          w.b_rb0 = c0 / 32;
           w.kt0 = kt0;
           w.nkt = n_kt;
-          w.ea = (const int*)d_eCb + (long long)mt * kTileM;
-          w.eb = d_eBd + (long long)nt * kTileN;
-          w.out = d_Kpart + (long long)k * nbf * nbf + (long long)mt * kTileM * nbf +
-                  (long long)nt * kTileN;
+          w.ea = (const int*)d_eCb + r0;
+          w.eb = d_eBd + c0;
+          w.out = d_Kpart + (long long)k * nbf * nbf + (long long)r0 * nbf + c0;
           w.ldr = nbf;
-          w.m_valid = std::min(kTileM, nbf - mt * kTileM);
-          w.n_valid = std::min(kTileN, nbf - nt * kTileN);
+          w.m_valid = std::min(kTileM, nbf - r0);
+          w.n_valid = std::min(kTileN, nbf - c0);
           items.push_back(w);
         }
     }

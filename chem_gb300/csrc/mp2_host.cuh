@@ -307,12 +307,15 @@ struct Mp2State {
     lv_nrb = cdiv_(vld, kTileN) * (kTileN / 32);
     lvdig_stride = (long long)lv_nrb * h_nkt * kSlices * kImage;
     w_nrb = std::max(cdiv_(naux, kTileM) * (kTileM / 32), cdiv_(naux, kTileN) * (kTileN / 32));
+    // Z tiles: a staircase over the upper triangle (column tiles of row
+    // tile r0 start at r0), fewer than on the grid
+    std::vector<std::pair<int, int>> ztiles;
+    for (int r0 = 0; r0 < naux; r0 += kTileM)
+      for (int c0 = r0; c0 < naux; c0 += kTileN) ztiles.push_back({r0, c0});
+    for (const auto& zt : ztiles) w_nrb = std::max(w_nrb, cdiv_(zt.second + kTileN, 32));
+    const int ntile = (int)ztiles.size();
     w_nkt = cdiv_(kw, kTileK);
     wdig_stride = (long long)w_nrb * w_nkt * kSlices * kImage;
-    int ntile = 0;
-    for (int mt = 0; mt < cdiv_(naux, kTileM); ++mt)
-      for (int nt = 0; nt < cdiv_(naux, kTileN); ++nt)
-        if ((nt + 1) * kTileN > mt * kTileM) ++ntile;
     const int ks = sp.choose_ksplit(w_nkt, ntile * npts);
     const int kt_per = cdiv_(w_nkt, ks);
     ksplit = cdiv_(w_nkt, kt_per);
@@ -474,26 +477,24 @@ struct Mp2State {
     for (int k = 0; k < ksplit; ++k) {
       const int kt0 = k * kt_per, n_kt = std::min(kt_per, w_nkt - kt0);
       for (int t = 0; t < npts; ++t)
-        for (int mt = 0; mt < cdiv_(naux, kTileM); ++mt)
-          for (int nt = 0; nt < cdiv_(naux, kTileN); ++nt) {
-            if ((nt + 1) * kTileN <= mt * kTileM) continue;  // strictly below the diagonal
+        for (const auto& zt : ztiles) {
+            const int r0 = zt.first, c0 = zt.second;
             SplitItem w = base_item();
             w.a = d_Wdig + t * wdig_stride;
             w.a_nrb = w_nrb;
-            w.a_rb0 = mt * (kTileM / 32);
+            w.a_rb0 = r0 / 32;
             w.b = w.a;
             w.b_nrb = w_nrb;
-            w.b_rb0 = nt * (kTileN / 32);
+            w.b_rb0 = c0 / 32;
             w.kt0 = kt0;
             w.nkt = n_kt;
             const int* eW = (const int*)d_eW + (long long)t * w_nrb * 32;
-            w.ea = eW + (long long)mt * kTileM;
-            w.eb = eW + (long long)nt * kTileN;
-            w.out = d_Zpart + ((long long)k * npts + t) * nn + (long long)mt * kTileM * naux +
-                    (long long)nt * kTileN;
+            w.ea = eW + r0;
+            w.eb = eW + c0;
+            w.out = d_Zpart + ((long long)k * npts + t) * nn + (long long)r0 * naux + c0;
             w.ldr = naux;
-            w.m_valid = std::min(kTileM, naux - mt * kTileM);
-            w.n_valid = std::min(kTileN, naux - nt * kTileN);
+            w.m_valid = std::min(kTileM, naux - r0);
+            w.n_valid = std::min(kTileN, naux - c0);
             items.push_back(w);
           }
     }

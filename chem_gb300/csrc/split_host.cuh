@@ -440,10 +440,15 @@ struct SplitState {
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    int ntile = 0;
-    for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
-      for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt)
-        if ((nt + 1) * kTileN > mt * kTileM) ++ntile;
+    // exchange output tiles: a staircase over the upper triangle, the
+    // column tiles of row tile r0 starting at column r0 (32-row operand
+    // blocks allow any multiple of 32); every (m, c >= m) lies in the row
+    // tile of m.  nbf 490: 15 tiles of 128 x 96 instead of 17 on the grid.
+    std::vector<std::pair<int, int>> ktiles;
+    for (int r0 = 0; r0 < nbf; r0 += kTileM)
+      for (int c0 = r0; c0 < nbf; c0 += kTileN) ktiles.push_back({r0, c0});
+    const int ntile = (int)ktiles.size();
+    for (const auto& t : ktiles) h_nrb = std::max(h_nrb, cdiv_(t.second + kTileN, 32));
     std::vector<int> sizes = {xb};
     const int xlast = naux - (nbatch - 1) * xb;
     if (xlast != xb) sizes.push_back(xlast);
@@ -521,25 +526,23 @@ struct SplitState {
       for (int ks = 0; ks < pl.ksplit; ++ks) {
         const int kt0 = ks * kt_per;
         const int n_kt = std::min(kt_per, nk_b - kt0);
-        for (int mt = 0; mt < cdiv_(nbf, kTileM); ++mt)
-          for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt) {
-            if ((nt + 1) * kTileN <= mt * kTileM) continue;  // strictly below the diagonal
+        for (const auto& t : ktiles) {
+            const int r0 = t.first, c0 = t.second;
             SplitItem w;
             w.a = d_Hslices;
             w.a_nrb = h_nrb;
-            w.a_rb0 = mt * (kTileM / 32);
+            w.a_rb0 = r0 / 32;
             w.b = d_Hslices;
             w.b_nrb = h_nrb;
-            w.b_rb0 = nt * (kTileN / 32);
+            w.b_rb0 = c0 / 32;
             w.kt0 = kt0;
             w.nkt = n_kt;
-            w.ea = d_eH + (long long)mt * kTileM;
-            w.eb = d_eH + (long long)nt * kTileN;
-            w.out = d_Kpart + (long long)ks * nbf * nbf + (long long)mt * kTileM * nbf +
-                    (long long)nt * kTileN;
+            w.ea = d_eH + r0;
+            w.eb = d_eH + c0;
+            w.out = d_Kpart + (long long)ks * nbf * nbf + (long long)r0 * nbf + c0;
             w.ldr = nbf;
-            w.m_valid = std::min(kTileM, nbf - mt * kTileM);
-            w.n_valid = std::min(kTileN, nbf - nt * kTileN);
+            w.m_valid = std::min(kTileM, nbf - r0);
+            w.n_valid = std::min(kTileN, nbf - c0);
             w.emax = nullptr;
             w.emax_row0 = 0;
             w.emax_div = 1;
