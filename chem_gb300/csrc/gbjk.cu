@@ -102,6 +102,26 @@ struct gbjk_ctx {
     double* d_H = nullptr;
     double* d_Kpart = nullptr;
   } fb;
+  // FP64 DF-MO / DF-LMO K with the occupied orbitals in batches
+  // (gbjk_set_occ_batch, megalochem's occ_nbatches): per batch the half
+  // transform of its columns, the fit and the split-K exchange, accumulated
+  // into K in batch order.  Per batch gs groups: nblk panels, nbf L^-1 fits,
+  // nbf V^-1 fits, the DF-MO and the DF-LMO exchange.  Index 0 of the
+  // per-size arrays is a full batch, 1 the shorter last one.
+  int occ_req = 0;
+  struct Fp64OccBatch {
+    int nocc = -1, ob = 0, nbatch = 0, olast = 0, gs = 0;
+    int ks[2] = {1, 1};
+    long long kc[2] = {0, 0};
+    bool elem_ht[2] = {false, false}, narrow[2] = {false, false}, elem_k[2] = {false, false};
+    int tn[2] = {64, 64};
+    int ht_t0[2] = {0, 0}, ht_nt[2] = {0, 0}, fit_t0[2] = {0, 0}, fit_nt[2] = {0, 0},
+        fitv_t0[2] = {0, 0}, mo_t0[2] = {0, 0}, mo_nt[2] = {0, 0}, lmo_t0[2] = {0, 0},
+        lmo_nt[2] = {0, 0};
+    GemmGroup* d_groups = nullptr;
+    GemmTile* d_tiles = nullptr;
+    double *d_H = nullptr, *d_H2 = nullptr, *d_Kpart = nullptr;
+  } ob;
   // launch configuration: requested (0 = built-in rule) and in effect
   gbjk_tunables tune{};
   gbjk_tunables tune_eff{};
@@ -606,6 +626,168 @@ gbjk_status ensure_k_batched(gbjk_ctx* ctx, int nocc) {
 
 gbjk_status filter(gbjk_ctx* ctx, double* M);
 
+// One grouped FP64 GEMM launch with the tile shape of a plan.
+void launch_fp64(cudaStream_t st, const GemmGroup* g, const GemmTile* t, int nt, bool elem,
+                 bool narrow, int tn, bool transB) {
+  if (nt == 0) return;
+  if (elem && transB)
+    k_gemm_fp64_elem<true><<<nt, 256, 0, st>>>(g, t, 1.0);
+  else if (elem)
+    k_gemm_fp64_elem<false><<<nt, 256, 0, st>>>(g, t, 1.0);
+  else if (transB)
+    k_gemm_fp64<true><<<nt, 256, 0, st>>>(g, t, 1.0);
+  else if (narrow)
+    k_gemm_fp64<false, false, 16><<<nt, 64, 0, st>>>(g, t, 1.0);
+  else if (tn == 32)
+    k_gemm_fp64<false, false, 32><<<nt, 128, 0, st>>>(g, t, 1.0);
+  else
+    k_gemm_fp64<false><<<nt, 256, 0, st>>>(g, t, 1.0);
+}
+
+// Occupied-batched FP64 exchange (DF-MO and DF-LMO): plans and buffers.
+gbjk_status ensure_k_occ_batched(gbjk_ctx* ctx, int nocc) {
+  auto& ob = ctx->ob;
+  if (ob.nocc == nocc) return GBJK_OK;
+  dfree(ctx, &ob.d_groups);
+  dfree(ctx, &ob.d_tiles);
+  dfree(ctx, &ob.d_H);
+  dfree(ctx, &ob.d_H2);
+  dfree(ctx, &ob.d_Kpart);
+  ob.nocc = -1;
+  gbjk_status s;
+  if ((s = ensure_c_workspace(ctx, nocc))) return s;
+  const int nbf = ctx->nbf, naux = ctx->naux, nblk = ctx->nblk;
+  ob.ob = std::min(nocc, ctx->occ_req);
+  ob.nbatch = cdiv(nocc, ob.ob);
+  ob.olast = nocc - (ob.nbatch - 1) * ob.ob;
+  ob.gs = nblk + 2 * nbf + 2;
+  const int sizes[2] = {ob.ob, ob.olast};
+  std::vector<GemmGroup> groups((size_t)ob.nbatch * ob.gs);
+  std::vector<GemmTile> tiles;
+  long long kmax = 1;
+  for (int v = 0; v < 2; ++v) {
+    const int obc = sizes[v];
+    Fp64Plan pl;
+    if ((s = fp64_plan(nbf, naux, obc, ctx->tune, &pl))) return fail(ctx, s, "invalid FP64 tunables");
+    ob.elem_ht[v] = pl.elem_ht;
+    ob.narrow[v] = pl.narrow;
+    ob.tn[v] = pl.ht_tn;
+    ob.elem_k[v] = pl.elem_k;
+    ob.ks[v] = pl.ks;
+    ob.kc[v] = pl.kc;
+    kmax = std::max<long long>(kmax, pl.ks);
+    const int tm = pl.elem_ht ? 16 : 64, kt = pl.elem_k ? 16 : 64;
+    ob.ht_t0[v] = (int)tiles.size();
+    for (int I = 0; I < nblk; ++I)
+      if (ctx->panelK[I])
+        add_tiles(tiles, I, ctx->bsize[I] * naux, obc, 0, ctx->panelK[I], 0, false, pl.ht_tn, tm);
+    ob.ht_nt[v] = (int)tiles.size() - ob.ht_t0[v];
+    ob.fit_t0[v] = (int)tiles.size();
+    for (int mu = 0; mu < nbf; ++mu)
+      add_tiles(tiles, nblk + mu, naux, obc, 0, naux, 0, false, pl.ht_tn, tm);
+    ob.fit_nt[v] = (int)tiles.size() - ob.fit_t0[v];
+    ob.fitv_t0[v] = (int)tiles.size();
+    for (int t = 0; t < ob.fit_nt[v]; ++t) {
+      GemmTile tt = tiles[ob.fit_t0[v] + t];
+      tt.group += nbf;
+      tiles.push_back(tt);
+    }
+    const long long kd = (long long)naux * obc;
+    for (int lmo = 0; lmo < 2; ++lmo) {
+      (lmo ? ob.lmo_t0[v] : ob.mo_t0[v]) = (int)tiles.size();
+      for (int k = 0; k < pl.ks; ++k) {
+        const int k0 = (int)(k * pl.kc), k1 = (int)std::min<long long>(kd, (k + 1) * pl.kc);
+        add_tiles(tiles, nblk + 2 * nbf + lmo, nbf, nbf, k0, std::max(k0, k1),
+                  (long long)k * nbf * nbf, !lmo, kt, kt);
+      }
+      (lmo ? ob.lmo_nt[v] : ob.mo_nt[v]) = (int)tiles.size() - (lmo ? ob.lmo_t0[v] : ob.mo_t0[v]);
+    }
+  }
+  const size_t hsz = (size_t)nbf * naux * ob.ob;
+  if ((s = dalloc(ctx, &ob.d_H, hsz)) || (s = dalloc(ctx, &ob.d_H2, hsz)) ||
+      (s = dalloc(ctx, &ob.d_Kpart, (size_t)kmax * nbf * nbf)))
+    return s;
+  for (int b = 0; b < ob.nbatch; ++b) {
+    const int i0 = b * ob.ob, obc = std::min(ob.ob, nocc - i0);
+    GemmGroup* g = groups.data() + (size_t)b * ob.gs;
+    for (int I = 0; I < nblk; ++I) {
+      const int K = ctx->panelK[I];
+      g[I] = {ctx->d_B + ctx->panel_off[I], ctx->d_Cg + (long long)ctx->cmoff[I] * nocc + i0,
+              ob.d_H + (long long)ctx->boff[I] * naux * obc, ctx->bsize[I] * naux, obc, K,
+              std::max(K, 1), nocc, obc, 0};
+    }
+    for (int mu = 0; mu < nbf; ++mu) {
+      const long long off = (long long)mu * naux * obc;
+      g[nblk + mu] = {ctx->d_Linv, ob.d_H + off, ob.d_H2 + off, naux, obc, naux, naux, obc, obc,
+                      kLowerA};
+      g[nblk + nbf + mu] = {ctx->d_Vinv, ob.d_H + off, ob.d_H2 + off, naux, obc, naux, naux, obc,
+                            obc, 0};
+    }
+    const int kd = naux * obc;
+    g[nblk + 2 * nbf] = {ob.d_H2, ob.d_H2, ob.d_Kpart, nbf, nbf, kd, kd, kd, nbf, kTransB};
+    // DF-LMO: K_nm = -sum Hfit[n] H[m]
+    g[nblk + 2 * nbf + 1] = {ob.d_H2, ob.d_H, ob.d_Kpart, nbf, nbf, kd, kd, kd, nbf, kTransB};
+  }
+  if ((s = dalloc(ctx, &ob.d_groups, groups.size()))) return s;
+  if ((s = dalloc(ctx, &ob.d_tiles, tiles.size()))) return s;
+  CK(cudaMemcpy(ob.d_groups, groups.data(), groups.size() * sizeof(GemmGroup),
+                cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ob.d_tiles, tiles.data(), tiles.size() * sizeof(GemmTile),
+                cudaMemcpyHostToDevice));
+  ctx->tune_eff.fp64_ht_tn = ob.elem_ht[0] ? 1 : ob.tn[0];
+  ctx->tune_eff.fp64_k_tile = ob.elem_k[0] ? 1 : 64;
+  ctx->tune_eff.fp64_kchunk = ob.kc[0];
+  ob.nocc = nocc;
+  return GBJK_OK;
+}
+
+gbjk_status run_k_occ_batched(gbjk_ctx* ctx, int kmethod, const double* dC, int nocc,
+                              double* dK) {
+  gbjk_status s;
+  if ((s = ensure_k_occ_batched(ctx, nocc))) return s;
+  auto& ob = ctx->ob;
+  const int nbf = ctx->nbf, nblk = ctx->nblk;
+  const bool mo = kmethod == GBJK_K_DFMO;
+  {
+    PhaseScope ps(ctx, PH_GATHER);
+    const long long total = (long long)ctx->ncols_total * nocc;
+    k_gather_cols<<<cdiv(total, 256), 256, 0, ctx->stream>>>(dC, nocc, ctx->d_colmap,
+                                                             ctx->ncols_total, ctx->d_Cg);
+    CKL(PH_GATHER);
+  }
+  for (int b = 0; b < ob.nbatch; ++b) {
+    const int v = (b == ob.nbatch - 1 && ob.olast != ob.ob) ? 1 : 0;
+    const GemmGroup* g = ob.d_groups + (size_t)b * ob.gs;
+    {
+      PhaseScope ps(ctx, PH_HT);
+      launch_fp64(ctx->stream, g, ob.d_tiles + ob.ht_t0[v], ob.ht_nt[v], ob.elem_ht[v],
+                  ob.narrow[v], ob.tn[v], false);
+      CKL(PH_HT);
+    }
+    {
+      PhaseScope ps(ctx, PH_FIT);
+      launch_fp64(ctx->stream, g, ob.d_tiles + (mo ? ob.fit_t0[v] : ob.fitv_t0[v]), ob.fit_nt[v],
+                  ob.elem_ht[v], ob.narrow[v], ob.tn[v], false);
+      CKL(PH_FIT);
+    }
+    {
+      PhaseScope ps(ctx, PH_KGEMM);
+      launch_fp64(ctx->stream, g, ob.d_tiles + (mo ? ob.mo_t0[v] : ob.lmo_t0[v]),
+                  mo ? ob.mo_nt[v] : ob.lmo_nt[v], ob.elem_k[v], false, 64, true);
+      CKL(PH_KGEMM);
+    }
+    {
+      PhaseScope ps(ctx, PH_KREDUCE);
+      const long long n2 = (long long)nbf * nbf;
+      k_splitk_reduce_acc<<<cdiv(n2, 256), 256, 0, ctx->stream>>>(
+          ob.d_Kpart, ob.ks[v], nbf, -1.0, mo ? 1 : 0, b > 0 ? 1 : 0, dK);
+      CKL(PH_KREDUCE);
+    }
+  }
+  (void)nblk;
+  return filter(ctx, dK);
+}
+
 gbjk_status run_k_batched(gbjk_ctx* ctx, const double* dC, int nocc, double* dK) {
   gbjk_status s;
   if ((s = ensure_k_batched(ctx, nocc))) return s;
@@ -921,7 +1103,8 @@ void gbjk_destroy(gbjk_ctx* ctx) {
   for (void* p : ptrs)
     if (p) cudaFree(p);
   for (void* p : {(void*)ctx->fb.d_groups, (void*)ctx->fb.d_tiles, (void*)ctx->fb.d_H,
-                  (void*)ctx->fb.d_Kpart})
+                  (void*)ctx->fb.d_Kpart, (void*)ctx->ob.d_groups, (void*)ctx->ob.d_tiles,
+                  (void*)ctx->ob.d_H, (void*)ctx->ob.d_H2, (void*)ctx->ob.d_Kpart})
     if (p) cudaFree(p);
   for (auto& pe : ctx->pending) {
     cudaEventDestroy(pe.second.first);
@@ -952,6 +1135,7 @@ gbjk_status gbjk_upload_b(gbjk_ctx* ctx, const double* B) {
   ctx->asymk.release();
   ctx->split.invalidate_b();
   ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
+  ctx->ob.nocc = -1;
   return GBJK_OK;
 }
 
@@ -970,6 +1154,7 @@ gbjk_status gbjk_upload_metric(gbjk_ctx* ctx, const double* Linv, const double* 
   ctx->asymk.release();
   ctx->split.invalidate_b();
   ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
+  ctx->ob.nocc = -1;
   return GBJK_OK;
 }
 
@@ -995,6 +1180,7 @@ gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted) {
   ctx->asymk.release();
   ctx->split.invalidate_b();
   ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
+  ctx->ob.nocc = -1;
   ctx->ws_nocc = -1;  // exchange plan reads H or the fitted H
   return GBJK_OK;
 }
@@ -1008,6 +1194,7 @@ gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows) {
   ctx->asymk.release();
   ctx->split.invalidate_b();
   ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
+  ctx->ob.nocc = -1;
   return GBJK_OK;
 }
 
@@ -1031,6 +1218,7 @@ gbjk_status gbjk_upload_b_synthetic(gbjk_ctx* ctx, unsigned long long seed, doub
   ctx->asymk.release();
   ctx->split.invalidate_b();
   ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
+  ctx->ob.nocc = -1;
   return GBJK_OK;
 }
 
@@ -1177,6 +1365,7 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
   ctx->asymk.release();
   ctx->split.invalidate_b();
   ctx->fb.nocc = -1;  // batched FP64 plans point into the tensor
+  ctx->ob.nocc = -1;
   return GBJK_OK;
 }
 
@@ -1194,6 +1383,14 @@ gbjk_status gbjk_test_split_stall(gbjk_ctx* ctx, int item, double wait_ms) {
   ctx->split.stop_item = item < 0 ? -1 : item;
   ctx->split.spin_ns = item < 0 ? kSpinNs : (unsigned long long)(wait_ms * 1e6);
   ctx->epoch++;  // kernel arguments of a captured build change
+  return GBJK_OK;
+}
+
+gbjk_status gbjk_set_occ_batch(gbjk_ctx* ctx, int cols) {
+  if (!ctx || cols < 0) return GBJK_INVALID_ARG;
+  if (cols != ctx->occ_req) ctx->epoch++;
+  ctx->occ_req = cols;
+  ctx->ob.nocc = -1;
   return GBJK_OK;
 }
 
@@ -1238,8 +1435,10 @@ gbjk_status gbjk_set_tunables(gbjk_ctx* ctx, const gbjk_tunables* t) {
       o.fp64_kchunk != t->fp64_kchunk)
     ctx->ws_nocc = -1;  // FP64 plans and workspaces are rebuilt at the next build
   if (o.fp64_ht_tn != t->fp64_ht_tn || o.fp64_k_tile != t->fp64_k_tile ||
-      o.fp64_kchunk != t->fp64_kchunk)
+      o.fp64_kchunk != t->fp64_kchunk) {
     ctx->fb.nocc = -1;
+    ctx->ob.nocc = -1;
+  }
   if (o.split_ksplit != t->split_ksplit) {
     ctx->split.ks_req = t->split_ksplit;
     ctx->split.release_build();
@@ -1497,6 +1696,10 @@ static gbjk_status check_ready(gbjk_ctx* ctx) {
 static bool fp64_batched(const gbjk_ctx* ctx) {
   return ctx->fitted && ctx->split.xb_req > 0 && ctx->split.xb_req < ctx->naux;
 }
+// FP64 exchange of an unfitted tensor in occupied batches
+static bool fp64_occ_batched(const gbjk_ctx* ctx, int nocc) {
+  return !ctx->fitted && ctx->occ_req > 0 && ctx->occ_req < nocc;
+}
 
 static gbjk_status prepare_split(gbjk_ctx* ctx, int nocc) {
   if (ctx->precision != GBJK_SPLIT_BF16) return GBJK_OK;
@@ -1591,10 +1794,13 @@ gbjk_status gbjk_compute_jk_dev(gbjk_ctx* ctx, int kmethod, const double* dP, co
       if ((s = prepare_split(ctx, nocc))) return s;
       return run_jk_split(ctx, dP, dC, nocc, dJ, dK);
     }
-    if (!fp64_batched(ctx) && (s = ensure_k_workspace(ctx, nocc))) return s;
+    if (!fp64_batched(ctx) && !fp64_occ_batched(ctx, nocc) &&
+        (s = ensure_k_workspace(ctx, nocc)))
+      return s;
   }
   if (dJ && (s = run_j(ctx, dP, dJ))) return s;
   if (dK && fp64_batched(ctx)) return run_k_batched(ctx, dC, nocc, dK);
+  if (dK && fp64_occ_batched(ctx, nocc)) return run_k_occ_batched(ctx, kmethod, dC, nocc, dK);
   if (dK && (s = run_k(ctx, kmethod, dC, nocc, dK))) return s;
   return GBJK_OK;
 }

@@ -82,6 +82,7 @@ def lib():
         L.gbjk_get_overlap.restype = C.c_int
         L.gbjk_set_fitted.argtypes = [vp, C.c_int]
         L.gbjk_set_aux_batch.argtypes = [vp, C.c_int]
+        L.gbjk_set_occ_batch.argtypes = [vp, C.c_int]
         L.gbjk_upload_b_synthetic.argtypes = [vp, C.c_ulonglong, C.c_double]
         L.gbjk_download_b.argtypes = [vp, dp]
         ip = C.POINTER(C.c_int)
@@ -334,6 +335,10 @@ class JKEngine:
         bounded waits run out and builds report TIMEOUT; -1 restores."""
         self._check(lib().gbjk_test_split_stall(self.h, int(item), float(wait_ms)),
                     "gbjk_test_split_stall")
+
+    def set_occ_batch(self, cols):
+        """FP64 K in occupied batches of `cols` orbitals (0: all at once)."""
+        self._check(lib().gbjk_set_occ_batch(self.h, int(cols)), "gbjk_set_occ_batch")
 
     def set_overlap(self, sms):
         """SMs the mixed-path exchange leaves to the concurrent J column

@@ -97,10 +97,21 @@ gbjk_status gbjk_set_precision(gbjk_ctx* ctx, int precision, int nslices);
  * synthetic DF-K workload, whose tensor is treated as pre-fitted.
  * No counterpart in the reference. */
 gbjk_status gbjk_set_fitted(gbjk_ctx* ctx, int fitted);
-/* Split path: process the auxiliary index in batches of `rows` (0 = all at
- * once; rounded down to a multiple of 32, at least 32), streaming the half transform and the exchange batch by batch so
- * that the half-transformed tensor never exists in full.  No counterpart in
- * the reference (it batches over X with DBCSR, src/fock/jkdf.cpp:412-422). */
+/* FP64 path, tensor not pre-fitted: build K (DF-MO or DF-LMO) with the
+ * occupied orbitals in batches of `cols` (0 = all at once), each batch's
+ * half transform, fit and exchange in turn, so that the half-transformed
+ * tensor exists for one batch only; the batch sums are added into K in
+ * order.  As megalochem batches the occupied index (occ_nbatches,
+ * src/fock/jkdf.cpp:254-268). */
+gbjk_status gbjk_set_occ_batch(gbjk_ctx* ctx, int cols);
+/* Process the auxiliary index in batches of `rows` (0 = all at once;
+ * rounded down to a multiple of 32, at least 32).  Split path: streaming
+ * the half transform and the exchange batch by batch so that the
+ * half-transformed tensor never exists in full.  No counterpart in the
+ * reference (it batches over X with DBCSR, src/fock/jkdf.cpp:412-422).
+ * FP64 path with a pre-fitted tensor (gbjk_set_fitted): the half transform
+ * and exchange of each batch in turn, the batch sums added into K in
+ * order. */
 gbjk_status gbjk_set_aux_batch(gbjk_ctx* ctx, int rows);
 /* Fill the panel array on the device with the seeded synthetic tensor
  * (Y, mu, nu) = N(0,1)[seed, min(mu,nu), max(mu,nu), Y] exp(-|I-J|/(2 decay)),

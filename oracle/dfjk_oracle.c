@@ -322,6 +322,58 @@ int oracle_dfmo_k_batched(const oracle_layout* L, const double* B, const double*
   return 0;
 }
 
+/* DF-MO (lmo = 0: HT2 = L^-1 HT, K = -HT2^T HT2) or DF-LMO (lmo = 1:
+ * HTfit = V^-1 HT, K_mn = -sum HTfit_m HT_n) K with the occupied orbitals in
+ * batches of ob (the last shorter), as the device's occupied-batched FP64
+ * path sums it: batch b covers orbitals [i0, i0 + obc); its reduction
+ * index t' = X*obc + (i - i0) runs in chunks of kc_full (kc_last for a
+ * shorter last batch), each an in-order fma sum, the chunk sums added in
+ * order to 0.0; the batch total is negated and added to K (K = -S_0, then
+ * K = -S_b + K).  M is L^-1 (lmo = 0, lower) or V^-1 (lmo = 1). */
+int oracle_dfk_occ_batched(const oracle_layout* L, const double* B, const double* M, int lmo,
+                           const double* Cm, int nocc, double* K, double eps, int ob,
+                           long long kc_full, long long kc_last) {
+  const int n = L->nbf, naux = L->naux;
+  if (ob <= 0 || kc_full <= 0 || kc_last <= 0) return 1;
+  const size_t sz = (size_t)n * naux * nocc;
+  double* H = (double*)malloc(sizeof(double) * sz);
+  double* H2 = (double*)malloc(sizeof(double) * sz);
+  if (!H || !H2) { free(H); free(H2); return 2; }
+  oracle_half_transform(L, B, Cm, nocc, H);
+  apply_metric(L, M, lmo ? 0 : 1, H, nocc, H2);
+  const double* A = H2;                /* rows mu */
+  const double* Bm = lmo ? H : H2;     /* rows nu */
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int mu = 0; mu < n; ++mu)
+    for (int nu = lmo ? 0 : mu; nu < n; ++nu) {
+      const double* a = A + (size_t)mu * naux * nocc;
+      const double* b = Bm + (size_t)nu * naux * nocc;
+      double k = 0.0;
+      for (int i0 = 0; i0 < nocc; i0 += ob) {
+        const int obc = i0 + ob < nocc ? ob : nocc - i0;
+        const long long kc = obc == ob ? kc_full : kc_last;
+        const long long len = (long long)naux * obc;
+        double s = 0.0;
+        for (long long t0 = 0; t0 < len; t0 += kc) {
+          const long long t1 = t0 + kc < len ? t0 + kc : len;
+          double p = 0.0;
+          for (long long t = t0; t < t1; ++t) {
+            const long long X = t / obc, i = i0 + t % obc;
+            p = fma(a[X * nocc + i], b[X * nocc + i], p);
+          }
+          s += p;
+        }
+        k = i0 == 0 ? -s : -s + k;
+      }
+      K[(size_t)mu * n + nu] = k;
+      if (!lmo) K[(size_t)nu * n + mu] = k;
+    }
+  oracle_filter(L, K, eps);
+  free(H);
+  free(H2);
+  return 0;
+}
+
 /* DF-LMO K (symmetric): HT = B C, HTfit = V^-1 HT, K_nm = -sum HT_m HTfit_n
  * (jkdf.cpp:1026-1088). */
 int oracle_dflmo_k(const oracle_layout* L, const double* B, const double* Vinv, const double* Cm,

@@ -54,6 +54,8 @@ def lib():
         L.oracle_dfmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
         L.oracle_dfmo_k_batched.argtypes = [lp, dp, dp, C.c_int, dp, C.c_double, C.c_int,
                                             C.c_longlong, C.c_longlong]
+        L.oracle_dfk_occ_batched.argtypes = [lp, dp, dp, C.c_int, dp, C.c_int, dp, C.c_double,
+                                             C.c_int, C.c_longlong, C.c_longlong]
         L.oracle_dflmo_k.argtypes = [lp, dp, dp, dp, C.c_int, dp, C.c_double, C.c_longlong]
         L.oracle_dfao_k.argtypes = [lp, dp, dp, dp, dp, C.c_double, C.c_longlong]
         L.oracle_half_transform.argtypes = [lp, dp, dp, C.c_int, dp]
@@ -128,6 +130,19 @@ class Oracle:
                                          _dp(K), eps, int(xb), int(kc_full), int(kc_last))
         if rc:
             raise RuntimeError(f"oracle_dfmo_k_batched failed ({rc})")
+        return K
+
+    def dfk_occ_batched(self, M, Cocc, ob, kc_full, kc_last, eps=0.0, lmo=False):
+        """DF-MO (M = L^-1) or DF-LMO (M = V^-1, lmo=True) K summed in
+        occupied batches of ob orbitals (the device's batched FP64 order)."""
+        C_ = np.ascontiguousarray(Cocc, float)
+        K = np.empty((self.layout.nbf, self.layout.nbf))
+        rc = lib().oracle_dfk_occ_batched(C.byref(self.L), _dp(self.B),
+                                          _dp(np.ascontiguousarray(M, float)), int(lmo), _dp(C_),
+                                          C_.shape[1], _dp(K), eps, int(ob), int(kc_full),
+                                          int(kc_last))
+        if rc:
+            raise RuntimeError(f"oracle_dfk_occ_batched failed ({rc})")
         return K
 
     def dflmo_k(self, Vinv, Cocc, eps=0.0, kchunk=0):

@@ -124,3 +124,29 @@ def test_fp64_bitwise_vs_oracle_c20h42():
     kc = k_split_plan(ds.nbf, ds.naux, ds.nocc)[1]
     assert np.array_equal(J, O.df_j(ds.Vinv, 2 * P, 1e-10))
     assert np.array_equal(K, O.dfmo_k(np.tril(ds.Linv), C, 1e-10, kchunk=kc))
+
+
+@pytest.mark.parametrize("sysname,ob", [("water", 3), ("butane", 8), ("decane", 16)])
+@pytest.mark.parametrize("kmethod", ["dfmo", "dflmo"])
+def test_fp64_occupied_batches_match_oracle(sysname, ob, kmethod, request):
+    """FP64 K with the occupied orbitals in batches (megalochem's
+    occ_nbatches): bit for bit the oracle's batched order, within rounding
+    of the unbatched K."""
+    from chem_gb300.fock import JKEngine, tune_plan
+    from oracle.oracle import Oracle
+    ds = request.getfixturevalue(sysname)
+    rng = np.random.default_rng(12)
+    C = np.ascontiguousarray(np.linalg.qr(rng.standard_normal((ds.nbf, ds.nbf)))[0][:, :ds.nocc])
+    eng = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=1e-10)
+    _, K0 = eng.compute_jk(None, C, kmethod)
+    eng.set_occ_batch(ob)
+    _, K1 = eng.compute_jk(None, C, kmethod)
+    eng.close()
+    olast = ds.nocc - (-(-ds.nocc // ob) - 1) * ob
+    kc_full = tune_plan(ds.nbf, ds.naux, ob)[0]["fp64_kchunk"]
+    kc_last = tune_plan(ds.nbf, ds.naux, olast)[0]["fp64_kchunk"]
+    M = np.tril(ds.Linv) if kmethod == "dfmo" else ds.Vinv
+    Kr = Oracle(ds.layout, ds.B).dfk_occ_batched(M, C, ob, kc_full, kc_last, 1e-10,
+                                                  lmo=kmethod == "dflmo")
+    assert np.array_equal(K1, Kr), np.abs(K1 - Kr).max()
+    assert np.abs(K1 - K0).max() <= 1e-12 * max(1.0, np.abs(K0).max())
