@@ -748,12 +748,18 @@ def main():
                 "ms_per_launch": per_launch_ms}
         if name == "split_gemm_ht":
             # algorithmic bytes of one launch: the digit slices of L^-1 B
-            # (five BF16 digits per tensor element, read once), the FP64
-            # H written (nocc columns) with the density-row partials, and
-            # the digit slices of C and of the density rows per panel
+            # (five BF16 digits per tensor element, read once), H written
+            # (five BF16 digits per element over auxiliary groups of 32 when
+            # the digits are cut in the epilogue, else FP64), the density-row
+            # partials (FP64), and the digit slices of C and of the density
+            # rows per panel
             lay = ds.layout
             cdig = sum(10.0 * int(k) * (nocc + int(b)) for k, b in zip(lay.panel_K, lay.bsizes))
-            byts = 10.0 * nnz + 8.0 * nbf * naux * (nocc + 1) + cdig
+            if eng.get_split_fuse():
+                hbytes = 10.0 * nbf * (-(-naux // 32) * 32) * nocc
+            else:
+                hbytes = 8.0 * nbf * naux * nocc
+            byts = 10.0 * nnz + hbytes + 8.0 * nbf * naux + cdig
             ai, ridge = f / byts, bf16 * 1e12 / (hbm * 1e9)
             if ai < ridge:  # below the ridge point: HBM bounds the launch
                 achb = byts / (per_launch_ms * 1e-3) / 1e9
@@ -762,9 +768,10 @@ def main():
                                                                "hbm_gbs)",
                              "algorithmic_bytes_per_launch": byts,
                              "bytes_definition": "10 B per tensor element (digit slices of "
-                                                 "L^-1 B) + 8 B per H element and density "
-                                                 "partial written + digit slices of C and "
-                                                 "the density rows",
+                                                 "L^-1 B) + H written (10 B digits per "
+                                                 "element, auxiliary index padded to 32; 8 B "
+                                                 "FP64 unfused) + 8 B per density partial + "
+                                                 "digit slices of C and the density rows",
                              "arithmetic_intensity_flop_per_byte": ai,
                              "ridge_flop_per_byte": ridge, "tensor_pipe": tensor})
     elif name in flops64:
@@ -1000,6 +1007,10 @@ def main():
                  if args.precision == "split" else "f64",
         "data": "synthetic molecule (seed-free alkane rule), host-computed integrals",
         "config": dict(workload_config(ds, mol, args.alkane, args.precision, world),
+                       h_digits="cut in the half-transform epilogue, exponent per (AO function, "
+                                "32 auxiliary indices)" if eng.get_split_fuse()
+                       else "separate pass over FP64 H, exponent per AO function"
+                       if args.precision == "split" else None,
                        autotune={"chosen": tune["chosen"], "best_ms": tune["best_ms"],
                                  "candidates": [(c["effective"], round(c["ms"], 4))
                                                 for c in tune["candidates"]]}),

@@ -323,13 +323,17 @@ struct AoKState {
     };
     i_ht0 = 0;
     for (int I = 0; I < nblk; ++I) {
-      const long long rows = (long long)(*L.bsize)[I] * naux;
+      // A rows (m, Y) at m * sp.apitch + Y (SplitItem::apitch)
+      const long long rows = (long long)(*L.bsize)[I] * sp.apitch;
       for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
         for (int nt = 0; nt < cdiv_(nbf, kTileN); ++nt) {
           SplitItem w = base();
           w.a = sp.d_Aslices + sp.a_off[I];
           w.a_nrb = sp.a_nrb[I];
           w.a_rb0 = mt * (kTileM / 32);
+          w.apitch = sp.apitch;
+          w.arow0 = mt * kTileM;
+          w.ay_valid = naux;
           w.b = d_Pdig + p_off[I];
           w.b_nrb = p_nrb;
           w.b_rb0 = nt * (kTileN / 32);

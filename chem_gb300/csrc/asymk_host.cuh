@@ -272,7 +272,8 @@ struct AsymKState {
     // from HBM once and from L2 for the other side
     i_ht0 = 0;
     for (int I = 0; I < nblk; ++I) {
-      const long long rows = (long long)(*L.bsize)[I] * naux;
+      // A rows (m, Y) at m * sp.apitch + Y (SplitItem::apitch)
+      const long long rows = (long long)(*L.bsize)[I] * sp.apitch;
       for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
         for (int side = 0; side < 2; ++side)
           for (int nt = 0; nt < cdiv_(nocc, kTileN); ++nt) {
@@ -280,6 +281,9 @@ struct AsymKState {
             w.a = sp.d_Aslices + sp.a_off[I];
             w.a_nrb = sp.a_nrb[I];
             w.a_rb0 = mt * (kTileM / 32);
+            w.apitch = sp.apitch;
+            w.arow0 = mt * kTileM;
+            w.ay_valid = naux;
             w.b = d_Cdig + side * cdig_side + c_off[I];
             w.b_nrb = c_nrb;
             w.b_rb0 = nt * (kTileN / 32);

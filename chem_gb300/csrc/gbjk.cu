@@ -1403,6 +1403,18 @@ gbjk_status gbjk_set_overlap(gbjk_ctx* ctx, int sms) {
   return GBJK_OK;
 }
 
+gbjk_status gbjk_set_split_fuse(gbjk_ctx* ctx, int on) {
+  if (!ctx) return GBJK_INVALID_ARG;
+  if (on != 0 && on != 1) return fail(ctx, GBJK_INVALID_ARG, "gbjk_set_split_fuse: 0 or 1");
+  if ((on != 0) != ctx->split.hfuse) {
+    ctx->epoch++;  // the launch sequence and the per-build buffers change
+    ctx->split.hfuse = on != 0;
+    ctx->split.release_build();
+  }
+  return GBJK_OK;
+}
+int gbjk_get_split_fuse(const gbjk_ctx* ctx) { return ctx ? (ctx->split.hfuse ? 1 : 0) : -1; }
+
 // --- launch configuration and autotuning -----------------------------------
 static gbjk_status check_ready(gbjk_ctx* ctx);
 
@@ -1472,9 +1484,11 @@ gbjk_status gbjk_tune_signature(const gbjk_ctx* ctx, int kmethod, int nocc, char
   long long ksum = 0;
   for (int k : ctx->panelK) ksum += k;
   std::snprintf(sig, len,
-                "gbjk1|%s|sm%d|prec%d|k%d|j%d|fit%d|xb%d|nbf%d|naux%d|nocc%d|nblk%d|nnz%lld|kp%lld",
+                "gbjk1|%s|sm%d|prec%d|k%d|j%d|fit%d|xb%d|hf%d|nbf%d|naux%d|nocc%d|nblk%d|nnz%lld|"
+                "kp%lld",
                 dev.c_str(), nsm, ctx->precision, kmethod, ctx->jmode, ctx->fitted ? 1 : 0,
-                ctx->split.xb_req, ctx->nbf, ctx->naux, nocc, ctx->nblk, ctx->nnz, ksum);
+                ctx->split.xb_req, ctx->split.hfuse ? 1 : 0, ctx->nbf, ctx->naux, nocc, ctx->nblk,
+                ctx->nnz, ksum);
   return GBJK_OK;
 }
 

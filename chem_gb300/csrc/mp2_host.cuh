@@ -423,7 +423,8 @@ struct Mp2State {
     // tile is read from HBM once for all points and then served from L2
     i1_0 = 0;
     for (int I = 0; I < nblk; ++I) {
-      const long long rows = (long long)bsize[I] * naux;
+      // A rows (m, Y) at m * sp.apitch + Y (SplitItem::apitch)
+      const long long rows = (long long)bsize[I] * sp.apitch;
       for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
         for (int t = 0; t < npts; ++t)
           for (int nt = 0; nt < cdiv_(ro[t], kTileN); ++nt) {
@@ -431,6 +432,9 @@ struct Mp2State {
             w.a = sp.d_Aslices + sp.a_off[I];
             w.a_nrb = sp.a_nrb[I];
             w.a_rb0 = mt * (kTileM / 32);
+            w.apitch = sp.apitch;
+            w.arow0 = mt * kTileM;
+            w.ay_valid = naux;
             w.b = d_Cdig + t * cdig_stride + cdig_off[I];
             w.b_nrb = c_nrb;
             w.b_rb0 = nt * (kTileN / 32);

@@ -110,6 +110,32 @@ struct SplitItem {
   // other order, provided every row uses the same one.
   long long perm_rs = 0;
   int perm_div = 1;
+  // Padded A rows.  apitch > 0: the A operand holds its panel rows (m, y) at
+  // R' = m * apitch + y (apitch a multiple of 32, so every 32-row block is
+  // one AO function m and one group of 32 auxiliary indices); the tile's
+  // row r is R' = arow0 + r, rows with y >= ay_valid are padding.  Every
+  // row-indexed output then uses the unpadded row R = m * ay_valid + y: the
+  // row-major `out` points at unpadded row arow0, emax/out2/perm take R.
+  int apitch = 0, arow0 = 0, ay_valid = 0;
+  // Half transform with digit output (k_split_gemm<true, false>): the
+  // tile's rows are (m, y) of one panel, its columns i orbitals.  Instead
+  // of FP64 values the epilogue writes the five digit slices of H row
+  // mu = hrow0 + m into `hdig` (h_nrb row blocks, 64-byte swizzled images,
+  // k-tile g * seg_nkt + i for auxiliary group g = y / 32, k = y % 32 in it)
+  // with one exponent per (mu, g), eseg[mu * es_ld + g], and the maximum
+  // over g into emax (biased, atomicMax).
+  uint16_t* hdig = nullptr;
+  int h_nrb = 0, hrow0 = 0;
+  int* eseg = nullptr;
+  int es_ld = 0;
+  // k-tiles per exponent segment (the orbital count of the half transform)
+  int seg_nkt = 0;
+  // Segmented exchange (k_split_gemm<false, true>): k-tile kt belongs to
+  // segment kt / seg_nkt, in which the tile's A and B rows carry the
+  // exponents esa[r * es_ld + g] and esb[c * es_ld + g] (ea/eb: their
+  // maxima over g).
+  const int* esa = nullptr;
+  const int* esb = nullptr;
 };
 
 // ------------------------------------------------------------ PTX helpers
@@ -193,6 +219,25 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   d |= (uint64_t)(512 >> 4) << 32;
   d |= (uint64_t)1 << 46;  // descriptor version (sm_100 family)
   return d;                // base offset 0, layout type 0 (no swizzle)
+}
+// smem matrix descriptor: K-major, 64-byte swizzle.  A row of 32 BF16 k
+// values is one 64-byte line; its 16-byte chunk c sits at chunk
+// c ^ ((row >> 1) & 3) (address bits 4-5 xor bits 7-8); 8-row groups are
+// 512 B apart (SBO).  The leading byte offset is unused in this mode.  The
+// second K = 16 step of a k-tile starts 32 B into the line.
+__device__ __forceinline__ uint64_t smem_desc_sw64(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(512 >> 4) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version (sm_100 family)
+  d |= (uint64_t)4 << 61;  // swizzle mode: 64-byte
+  return d;
+}
+// Element offset (in BF16 units) of (row r, k) inside a 32 x 32 slice image
+// in the 64-byte swizzled layout.
+__host__ __device__ __forceinline__ int sw64_offset(int r, int k) {
+  return r * 32 + ((((k >> 3) ^ ((r >> 1) & 3))) << 3) + (k & 7);
 }
 // instruction descriptor: kind::f16, BF16 x BF16 -> F32, K-major A and B
 __host__ __device__ constexpr uint32_t instr_desc(int M, int N) {
@@ -280,6 +325,13 @@ __device__ __forceinline__ double i64_scaled_to_f64(long long v, int e2) {
   return __longlong_as_double(v == 0 ? 0ll : r);
 }
 
+// x * 2^-sh rounded to nearest (ties up) for sh >= 0; 0 when sh > 62.
+__device__ __forceinline__ long long shr_round(long long x, int sh) {
+  if (sh == 0) return x;
+  if (sh > 62) return 0;
+  return (x + (1ll << (sh - 1))) >> sh;
+}
+
 // ------------------------------------------------------------ split kernels
 // A split job fills rows [row0, row0 + nrows) of one digit operand:
 // element (r, c) = src[(r - row0)*rs + c*cs] for c < ncols, zero for
@@ -314,6 +366,13 @@ __global__ void k_row_maxexp(const SplitJob* __restrict__ jobs) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   if (lane == 0) jb.e[jb.row0 + i] = mx == 0 ? -2000 : (int)mx - 1022;
+}
+
+// p[i] = v for i < n (grid-stride).
+__global__ void k_fill_int(int* __restrict__ p, long long n, int v) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    p[i] = v;
 }
 
 // Biased FP64 exponent maxima (0 = all zero) -> row exponents in place.
@@ -405,7 +464,20 @@ __global__ void k_split_tiles(const SplitJob* __restrict__ jobs) {
 // ------------------------------------------------------------ the GEMM
 // Pairs (s, t) are issued exact diagonals first (d = 0, 1, 2), then d = 3, 4;
 // the accumulator of diagonal d sits at TMEM column d * kTileN.
+//
+// Variants.  kHDigits: the half transform writes H as digit slices
+// (SplitItem::hdig) with one exponent per (AO function, auxiliary group)
+// instead of FP64 values.  kSeg: the exchange over such digits; its
+// operands are 64-byte swizzled and its k range is cut into segments of
+// seg_nkt k-tiles, each with its own row exponents.  An exact chunk never
+// crosses a segment boundary, the diagonals 3 and 4 are reset at every
+// segment start and folded in at its end, and every chunk and fold is added
+// to the int64 result in units of 2^(eA+eB-46) of the rows' maximum
+// exponents eA, eB, shifted right by (eA - eA_g) + (eB - eB_g) bits with
+// rounding (exact while that shift is at most 16 for a chunk, 0 for a
+// fold).  Without kSeg there is one segment per item and no shift.
 
+template <bool kHDigits, bool kSeg>
 __global__ void __launch_bounds__(kThreads, 1)
     k_split_gemm(const SplitItem* __restrict__ items, int nitems, int* __restrict__ err,
                  int stop_item, unsigned long long spin_ns) {
@@ -417,6 +489,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   unsigned char* sB = smem + kStages * kBytesA;   // kStages * kBytesB
   __shared__ uint64_t full_bar[kStages], empty_bar[kStages];
   __shared__ uint64_t exact_full, exact_empty, final_full, final_empty, mma_drain;
+  // kHDigits: the three epilogue warps of a TMEM lane quadrant combine their
+  // exponent maxima (double-buffered by item parity)
+  __shared__ uint64_t grp_bar[4];
+  __shared__ int grp_max[2][4][3];
   __shared__ uint32_t tmem_base_sh;
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -430,6 +506,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     mbar_init(&final_full, 1);
     mbar_init(&final_empty, kEpiWarps);
     mbar_init(&mma_drain, 1);
+    for (int i = 0; i < 4; ++i) mbar_init(&grp_bar[i], 3);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -498,23 +575,32 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool ok = true;
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
         const SplitItem w = items[it];
+        const int seg = kSeg ? w.seg_nkt : (1 << 30);
+        int o = kSeg ? w.kt0 % seg : 0;  // position of the k-tile in its segment
         for (int k = 0; k < w.nkt && ok; ++k) {
-          const bool chunk_start = (k % kChunkTiles) == 0;
-          const bool chunk_end = ((k + 1) % kChunkTiles) == 0 || k + 1 == w.nkt;
+          const bool seg_start = k == 0 || o == 0;
+          const bool chunk_start = seg_start || (o % kChunkTiles) == 0;
+          const bool seg_end = k + 1 == w.nkt || o + 1 == seg;
+          const bool chunk_end = seg_end || ((o + 1) % kChunkTiles) == 0;
           ok = mbar_wait(&full_bar[stage], phase, err, 5, spin_ns);
           if (!ok) break;
           tc_fence_after();
-          const uint64_t adesc = smem_desc(smem_u32(sA + stage * kBytesA));
-          const uint64_t bdesc = smem_desc(smem_u32(sB + stage * kBytesB));
+          const uint32_t a_addr = smem_u32(sA + stage * kBytesA);
+          const uint32_t b_addr = smem_u32(sB + stage * kBytesB);
+          const uint64_t adesc = kSeg ? smem_desc_sw64(a_addr) : smem_desc(a_addr);
+          const uint64_t bdesc = kSeg ? smem_desc_sw64(b_addr) : smem_desc(b_addr);
           // descriptor start addresses advance in 16-byte units
           constexpr uint32_t kSliceA = kTileM * kTileK * 2 / 16, kSliceB = kTileN * kTileK * 2 / 16;
+          // the second K = 16 step of the k-tile: two core matrices on
+          // (256 B) unswizzled, 32 B into each 64-byte line swizzled
+          constexpr uint32_t kStepK = kSeg ? 2 : 16;
           // The 15 slice pairs (s, t), s + t <= 4, as 9 MMAs: B slices t0 and
           // t0+1 are adjacent in shared memory and diagonals d and d+1 have
           // adjacent accumulators, so one N = 192 MMA updates both.  Entries:
           // {s, t0, number of B slices, reset class}; reset class 1 = first
           // write of exact diagonals (reset at a chunk start), 2 = first write
-          // of d = 3, 4 (reset at the item's first k-tile).  MMAs 0..3 cover
-          // exactly the diagonals 0..2, MMAs 4..8 the diagonals 3 and 4.
+          // of d = 3, 4 (reset at a segment start).  MMAs 0..3 cover exactly
+          // the diagonals 0..2, MMAs 4..8 the diagonals 3 and 4.
           auto issue = [&](int q0, int q1) {
 #pragma unroll
             for (int q = 0; q < 9; ++q) {
@@ -525,20 +611,20 @@ __global__ void __launch_bounds__(kThreads, 1)
               if (q < q0 || q >= q1) continue;
               const uint32_t dcol = tmem + (uint32_t)((qs[q] + qt[q]) * kTileN);
               const uint32_t id = qn[q] == 2 ? idesc2 : idesc;
-              const bool reset = qr[q] == 1 ? chunk_start : (qr[q] == 2 ? k == 0 : false);
+              const bool reset = qr[q] == 1 ? chunk_start : (qr[q] == 2 ? seg_start : false);
 #pragma unroll
               for (int j = 0; j < 2; ++j) {
-                const uint64_t ad = adesc + (uint64_t)(qs[q] * kSliceA + j * 16);
-                const uint64_t bd = bdesc + (uint64_t)(qt[q] * kSliceB + j * 16);
+                const uint64_t ad = adesc + (uint64_t)(qs[q] * kSliceA + j * kStepK);
+                const uint64_t bd = bdesc + (uint64_t)(qt[q] * kSliceB + j * kStepK);
                 mma_bf16(dcol, ad, bd, id, (reset && j == 0) ? 0u : 1u);
               }
             }
           };
-          if (k == 0) {
-            // item start: the exact diagonals are free once the epilogue has
-            // drained the previous item's last chunk, which comes before its
-            // fold of d = 3, 4; so the exact pairs go first and overlap that
-            // fold, and the d = 3, 4 pairs wait for it
+          if (seg_start) {
+            // segment (item) start: the exact diagonals are free once the
+            // epilogue has drained the previous segment's last chunk, which
+            // comes before its fold of d = 3, 4; so the exact pairs go first
+            // and overlap that fold, and the d = 3, 4 pairs wait for it
             ok = mbar_wait(&exact_empty, ex_phase ^ 1, err, 4, spin_ns);
             ex_phase ^= 1;
             if (!ok) {
@@ -555,7 +641,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
             issue(4, 9);
           } else if (chunk_start) {
-            // d = 3, 4 first: they accumulate over the whole item and the
+            // d = 3, 4 first: they accumulate over the whole segment and the
             // exact drain does not read them, so they overlap the epilogue's
             // drain of the previous chunk; the exact pairs wait for it
             issue(4, 9);
@@ -573,12 +659,13 @@ __global__ void __launch_bounds__(kThreads, 1)
             issue(4, 9);
           }
           mma_commit(&empty_bar[stage]);
+          if (seg_end) mma_commit(&final_full);
           if (++stage == kStages) {
             stage = 0;
             phase ^= 1;
           }
+          if (++o == seg) o = 0;
         }
-        if (ok) mma_commit(&final_full);
       }
       // every MMA this thread issued completes before TMEM is freed and the
       // CTA exits, also after a timeout (commit tracks all prior MMAs)
@@ -588,10 +675,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   } else {
     // ---------------- epilogue (warps 2..13)
     const int q = warp & 3;                 // TMEM lane quadrant of this warp
-    const int half = (warp - 2) >> 2;       // column third: 0, 1 or 2
+    const int third = (warp - 2) >> 2;      // column third: 0, 1 or 2
     const int row = q * 32 + lane;          // tile-local row
     const uint32_t lane_addr = (uint32_t)(q * 32) << 16;
-    uint32_t ex_phase = 0, fin_phase = 0;
+    uint32_t ex_phase = 0, fin_phase = 0, grp_phase = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
       const SplitItem& w = items[it];  // fields read where used (register pressure)
@@ -599,24 +686,20 @@ __global__ void __launch_bounds__(kThreads, 1)
       // warp's 32 columns (one per lane, broadcast by shuffles at the store),
       // loaded now so that their latency hides behind the drains; a tile's
       // 128 A rows and 96 B rows are always allocated
-      const int cbase = half * kEpiCols;
+      const int cbase = third * kEpiCols;
       const int er = w.ea[row];
       const int ecl = w.eb[cbase + lane];
       long long V[kEpiCols];
 #pragma unroll
       for (int c = 0; c < kEpiCols; ++c) V[c] = 0;
-      const int nchunks = (w.nkt + kChunkTiles - 1) / kChunkTiles;
-      for (int ch = 0; ch < nchunks && ok; ++ch) {
-        ok = mbar_wait(&exact_full, ex_phase, err, 6, spin_ns);
-        ex_phase ^= 1;
-        if (!ok) break;
-        tc_fence_after();
+      // exact diagonals of one chunk into V (kSeg: shifted by sh_a + sh_b)
+      auto drain = [&](int sh_a, int sh_b) {
         // d0 is at most 2^22 in magnitude: converted with the 1.5*2^23 magic
         // (one FADD); d1, d2 (below 2^24) with a rounding conversion
 #pragma unroll
         for (int g = 0; g < kEpiCols / 16; ++g) {
           uint32_t v0[16], v1[16], v2[16];
-          const uint32_t col = (uint32_t)(half * kEpiCols + g * 16);
+          const uint32_t col = (uint32_t)(third * kEpiCols + g * 16);
           tmem_ld16(tmem + lane_addr + col, v0);
           tmem_ld16(tmem + lane_addr + (uint32_t)kTileN + col, v1);
           tmem_ld16(tmem + lane_addr + (uint32_t)(2 * kTileN) + col, v2);
@@ -627,109 +710,244 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int r1 = __float2int_rn(__uint_as_float(v1[c]));
             const int r2 = __float2int_rn(__uint_as_float(v2[c]));
             const int t01 = (r0 << 8) + r1;  // < 2^31
-            V[g * 16 + c] += ((long long)t01 << 8) + r2;
+            const long long wc = ((long long)t01 << 8) + r2;
+            if constexpr (kSeg) {
+              const int sh = sh_a + __shfl_sync(0xffffffffu, sh_b, g * 16 + c);
+              V[g * 16 + c] += sh <= 16 ? (wc << (16 - sh)) : shr_round(wc, sh - 16);
+            } else {
+              V[g * 16 + c] += wc;
+            }
           }
         }
         tc_fence_before();
         __syncwarp();
         if (lane == 0) mbar_arrive(&exact_empty);
-      }
-      if (!ok) break;
-      ok = mbar_wait(&final_full, fin_phase, err, 7, spin_ns);
-      fin_phase ^= 1;
-      if (!ok) break;
-      tc_fence_after();
-      // fold the approximate diagonals in with 16 fractional bits:
+      };
+      // fold the approximate diagonals in with 16 fractional bits,
       //   V = W 2^16 + rint(256 r3) + rint(r4),  value = V 2^(eA+eB-46)
+      // (kSeg: the segment's part, shifted, added to V)
+      auto fold = [&](int sh_a, int sh_b) {
 #pragma unroll
-      for (int g = 0; g < kEpiCols / 16; ++g) {
-        uint32_t v3[16], v4[16];
-        tmem_ld16(tmem + lane_addr + (uint32_t)(3 * kTileN + half * kEpiCols + g * 16), v3);
-        tmem_ld16(tmem + lane_addr + (uint32_t)(4 * kTileN + half * kEpiCols + g * 16), v4);
-        tmem_wait_ld();
+        for (int g = 0; g < kEpiCols / 16; ++g) {
+          uint32_t v3[16], v4[16];
+          tmem_ld16(tmem + lane_addr + (uint32_t)(3 * kTileN + third * kEpiCols + g * 16), v3);
+          tmem_ld16(tmem + lane_addr + (uint32_t)(4 * kTileN + third * kEpiCols + g * 16), v4);
+          tmem_wait_ld();
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-          int h3, l3, h4, l4;
-          f32_split16(__fmul_rn(__uint_as_float(v3[c]), 256.0f), h3, l3);
-          f32_split16(__uint_as_float(v4[c]), h4, l4);
-          V[g * 16 + c] = ((V[g * 16 + c] + (long long)(h3 + h4)) << 16) + (long long)(l3 + l4);
+          for (int c = 0; c < 16; ++c) {
+            int h3, l3, h4, l4;
+            f32_split16(__fmul_rn(__uint_as_float(v3[c]), 256.0f), h3, l3);
+            f32_split16(__uint_as_float(v4[c]), h4, l4);
+            if constexpr (kSeg) {
+              const int sh = sh_a + __shfl_sync(0xffffffffu, sh_b, g * 16 + c);
+              const long long f = ((long long)(h3 + h4) << 16) + (long long)(l3 + l4);
+              V[g * 16 + c] += shr_round(f, sh);
+            } else {
+              V[g * 16 + c] =
+                  ((V[g * 16 + c] + (long long)(h3 + h4)) << 16) + (long long)(l3 + l4);
+            }
+          }
         }
+        // the accumulators are free for the next segment or item
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&final_empty);
+      };
+      if constexpr (kSeg) {
+        const int nkt = w.nkt, seg = w.seg_nkt;
+        int o = w.kt0 % seg;  // position in the segment
+        int sh_a = 0, sh_b = 0;  // shifts of this row and of column cbase + lane
+        for (int k = 0; k < nkt && ok;) {
+          const int len = min(min(kChunkTiles - o % kChunkTiles, seg - o), nkt - k);
+          if (k == 0 || o == 0) {
+            const int g = (w.kt0 + k) / seg;
+            const int ea_g = w.esa[row * w.es_ld + g];
+            const int eb_g = w.esb[(cbase + lane) * w.es_ld + g];
+            sh_a = (er <= -2000 || ea_g <= -2000) ? 4096 : max(0, er - ea_g);
+            sh_b = (ecl <= -2000 || eb_g <= -2000) ? 4096 : max(0, ecl - eb_g);
+          }
+          ok = mbar_wait(&exact_full, ex_phase, err, 6, spin_ns);
+          ex_phase ^= 1;
+          if (!ok) break;
+          tc_fence_after();
+          drain(sh_a, sh_b);
+          k += len;
+          o += len;
+          if (k == nkt || o == seg) {
+            ok = mbar_wait(&final_full, fin_phase, err, 7, spin_ns);
+            fin_phase ^= 1;
+            if (!ok) break;
+            tc_fence_after();
+            fold(sh_a, sh_b);
+            if (o == seg) o = 0;
+          }
+        }
+      } else {
+        const int nchunks = (w.nkt + kChunkTiles - 1) / kChunkTiles;
+        for (int ch = 0; ch < nchunks && ok; ++ch) {
+          ok = mbar_wait(&exact_full, ex_phase, err, 6, spin_ns);
+          ex_phase ^= 1;
+          if (!ok) break;
+          tc_fence_after();
+          drain(0, 0);
+        }
+        if (!ok) break;
+        ok = mbar_wait(&final_full, fin_phase, err, 7, spin_ns);
+        fin_phase ^= 1;
+        if (!ok) break;
+        tc_fence_after();
+        fold(0, 0);
       }
-      // the accumulators are free for the next item before the stores
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&final_empty);
+      if (!ok) break;
       // item fields of the store phase, loaded together so their latencies
       // overlap
       const int m_valid = w.m_valid, n_valid = w.n_valid, ncol1 = w.ncol1, c0 = w.c0;
       const int emax_row0 = w.emax_row0, emax_div = w.emax_div, perm_div = w.perm_div;
+      const int apitch = w.apitch, arow0 = w.arow0, ay_valid = w.ay_valid;
       double* const out = w.out;
       double* const out2 = w.out2;
       const long long ldr = w.ldr, perm_rs = w.perm_rs;
-      const bool rvalid = row < m_valid;
-      unsigned int emax_row = 0;
-      {
-        const bool perm = perm_rs != 0;
-        double* orow;
-        if (perm) {
-          const int R = emax_row0 + row;
-          const int m = R / perm_div, y = R - m * perm_div;
-          orow = out + (long long)m * perm_rs + (long long)(y & ~31) * ldr +
-                 ((y & 31) * 2 + (cbase >> 1) * 64);
-        } else {
-          orow = out + (long long)row * ldr + cbase;
-        }
-        const bool vec = ((uintptr_t)orow & 15) == 0;
-        const int nstore = min(n_valid, ncol1 - c0);  // columns kept in `out`
-        // density column of this row's AO function (tile-local), or -1
-        int dcol = -1;
-        if (out2) {
-          const int cand = ncol1 + (emax_row0 + row) / emax_div - c0;
-          if (cand >= 0 && cand < n_valid) dcol = cand;
-        }
+      const bool rin = row < m_valid;  // row inside the tile
+      // unpadded panel row R of this row, its offset from the row-major
+      // output's first row, and whether it is a real row (not padding)
+      int R = emax_row0 + row, mloc = 0, yrow = 0;
+      long long rofs = row;
+      bool rvalid = rin;
+      if (apitch) {
+        const int Rp = arow0 + row;
+        mloc = Rp / apitch;
+        yrow = Rp - mloc * apitch;
+        rvalid = rin && yrow < ay_valid;
+        R = mloc * ay_valid + yrow;
+        rofs = (long long)R - arow0;
+      }
+      const int nstore = min(n_valid, ncol1 - c0);  // columns kept in `out`
+      // density column of this row's AO function (tile-local), or -1
+      int dcol = -1;
+      if (out2) {
+        const int cand = ncol1 + R / emax_div - c0;
+        if (cand >= 0 && cand < n_valid) dcol = cand;
+      }
+      if constexpr (kHDigits) {
+        // The warp's 32 rows are one auxiliary group g of one AO function
+        // (apitch is a multiple of 32 and tiles start at multiples of 128):
+        // its exponent is the maximum over these rows and the quadrant's
+        // columns, eg = max (bit length of |V| + er + ec - 46), so that
+        // |value| < 2^eg for every value of the group.
+        int emx = -2000;
 #pragma unroll
-        for (int c = 0; c < kEpiCols; c += 2) {
-          const int ecs0 = __shfl_sync(0xffffffffu, ecl, c);
-          const int ecs1 = __shfl_sync(0xffffffffu, ecl, c + 1);
+        for (int c = 0; c < kEpiCols; ++c) {
+          const int ec = __shfl_sync(0xffffffffu, ecl, c);
           const int col = cbase + c;
-          const bool s0 = rvalid && col < nstore, s1 = rvalid && col + 1 < nstore;
-          const bool d0 = rvalid && col == dcol, d1 = rvalid && col + 1 == dcol;
-          if (!(s0 || s1 || d0 || d1)) continue;
-          const int ec0 = (s0 || d0) ? ecs0 : -2000;
-          const int ec1 = (s1 || d1) ? ecs1 : -2000;
-          const double x0 =
-              (er <= -2000 || ec0 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c], er + ec0 - 46);
-          const double x1 =
-              (er <= -2000 || ec1 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c + 1], er + ec1 - 46);
-          if (d0) out2[emax_row0 + row] = x0;
-          if (d1) out2[emax_row0 + row] = x1;
-          if (s0) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x0) >> 52) & 0x7FF));
-          if (s1) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x1) >> 52) & 0x7FF));
-          if (perm) {
-            // the pair's second column is the zero pad column when nstore
-            // is odd (the last orbital of an odd count)
-            if (s0)
-              *reinterpret_cast<double2*>(orow + (c >> 1) * 64) = make_double2(x0, s1 ? x1 : 0.0);
-          } else if (vec && s0 && s1) {
-            *reinterpret_cast<double2*>(orow + c) = make_double2(x0, x1);
-          } else {
-            if (s0) orow[c] = x0;
-            if (s1) orow[c + 1] = x1;
+          if (rvalid && col == dcol)
+            out2[R] = (er <= -2000 || ec <= -2000) ? 0.0 : i64_scaled_to_f64(V[c], er + ec - 46);
+          if (rvalid && col < nstore && V[c] != 0 && er > -2000 && ec > -2000) {
+            const unsigned long long a =
+                V[c] < 0 ? (unsigned long long)(-V[c]) : (unsigned long long)V[c];
+            emx = max(emx, (64 - __clzll((long long)a)) + er + ec - 46);
           }
         }
-      }
-      if (unsigned int* const emaxp = w.emax) {
-        // one atomic per warp when all its rows map to the same target row
-        const int target = rvalid ? (emax_row0 + row) / emax_div : -1;
-        const int t0 = __shfl_sync(0xffffffffu, target, 0);
-        const bool same = __all_sync(0xffffffffu, target == t0);
-        if (same) {
-          unsigned int m = emax_row;
+        emx = __reduce_max_sync(0xffffffffu, emx);
+        const int gp = (int)grp_phase;
+        if (lane == 0) grp_max[gp][q][third] = emx;
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&grp_bar[q]);
+        ok = mbar_wait(&grp_bar[q], grp_phase, err, 8, spin_ns);
+        grp_phase ^= 1;
+        if (!ok) break;
+        const int eg = max(max(grp_max[gp][q][0], grp_max[gp][q][1]), grp_max[gp][q][2]);
+        const int mu = w.hrow0 + mloc;
+        const int gy = yrow >> 5;
+        if (third == 0 && lane == 0 && rin) {
+          w.eseg[(long long)mu * w.es_ld + gy] = eg;
+          if (eg > -2000 && w.emax) atomicMax(w.emax + mloc, (unsigned int)max(1, eg + 1022));
+        }
+        if (rin) {
+          // digit slices of X = rint(|value| 2^(39-eg)) (see the number
+          // format above) straight from the integer V: value = V 2^(er+ec-46)
+          const long long sstride = (long long)w.h_nrb * kImage;
+          const long long tstride = (long long)kSlices * sstride;
+          uint16_t* const hbase =
+              w.hdig + (long long)(mu >> 5) * kImage + sw64_offset(mu & 31, lane);
+          const long long kt0 = (long long)gy * w.seg_nkt + c0;
 #pragma unroll
-          for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-          if (lane == 0 && t0 >= 0 && m) atomicMax(emaxp + t0, m);
-        } else if (target >= 0 && emax_row) {
-          atomicMax(emaxp + target, emax_row);
+          for (int c = 0; c < kEpiCols; ++c) {
+            const int ec = __shfl_sync(0xffffffffu, ecl, c);
+            const int col = cbase + c;
+            if (col >= nstore) continue;  // the same for the whole warp
+            const long long v = V[c];
+            unsigned long long X = 0;
+            if (rvalid && v != 0 && er > -2000 && ec > -2000 && eg > -2000) {
+              const unsigned long long a = v < 0 ? (unsigned long long)(-v) : (unsigned long long)v;
+              const int t = eg - (er + ec - 46) - 39;
+              X = t <= 0 ? (a << (-t)) : (t > 63 ? 0ull : (a + (1ull << (t - 1))) >> t);
+            }
+            const unsigned long long T = X + 0x80808080ull;
+            uint16_t* const p = hbase + (kt0 + col) * tstride;
+#pragma unroll
+            for (int s = 0; s < kSlices; ++s) {
+              const int d = s == 0 ? (int)(T >> 32) : (int)((T >> (8 * (4 - s))) & 255) - 128;
+              p[s * sstride] = small_int_to_bf16(v < 0 ? -d : d);
+            }
+          }
+        }
+      } else {
+        unsigned int emax_row = 0;
+        {
+          const bool perm = perm_rs != 0;
+          double* orow;
+          if (perm) {
+            const int m = R / perm_div, y = R - m * perm_div;
+            orow = out + (long long)m * perm_rs + (long long)(y & ~31) * ldr +
+                   ((y & 31) * 2 + (cbase >> 1) * 64);
+          } else {
+            orow = out + rofs * ldr + cbase;
+          }
+          const bool vec = ((uintptr_t)orow & 15) == 0;
+#pragma unroll
+          for (int c = 0; c < kEpiCols; c += 2) {
+            const int ecs0 = __shfl_sync(0xffffffffu, ecl, c);
+            const int ecs1 = __shfl_sync(0xffffffffu, ecl, c + 1);
+            const int col = cbase + c;
+            const bool s0 = rvalid && col < nstore, s1 = rvalid && col + 1 < nstore;
+            const bool d0 = rvalid && col == dcol, d1 = rvalid && col + 1 == dcol;
+            if (!(s0 || s1 || d0 || d1)) continue;
+            const int ec0 = (s0 || d0) ? ecs0 : -2000;
+            const int ec1 = (s1 || d1) ? ecs1 : -2000;
+            const double x0 =
+                (er <= -2000 || ec0 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c], er + ec0 - 46);
+            const double x1 =
+                (er <= -2000 || ec1 <= -2000) ? 0.0 : i64_scaled_to_f64(V[c + 1], er + ec1 - 46);
+            if (d0) out2[R] = x0;
+            if (d1) out2[R] = x1;
+            if (s0) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x0) >> 52) & 0x7FF));
+            if (s1) emax_row = max(emax_row, (unsigned int)((__double_as_longlong(x1) >> 52) & 0x7FF));
+            if (perm) {
+              // the pair's second column is the zero pad column when nstore
+              // is odd (the last orbital of an odd count)
+              if (s0)
+                *reinterpret_cast<double2*>(orow + (c >> 1) * 64) = make_double2(x0, s1 ? x1 : 0.0);
+            } else if (vec && s0 && s1) {
+              *reinterpret_cast<double2*>(orow + c) = make_double2(x0, x1);
+            } else {
+              if (s0) orow[c] = x0;
+              if (s1) orow[c + 1] = x1;
+            }
+          }
+        }
+        if (unsigned int* const emaxp = w.emax) {
+          // one atomic per warp when all its rows map to the same target row
+          const int target = rvalid ? R / emax_div : -1;
+          const int t0 = __shfl_sync(0xffffffffu, target, 0);
+          const bool same = __all_sync(0xffffffffu, target == t0);
+          if (same) {
+            unsigned int m = emax_row;
+#pragma unroll
+            for (int o2 = 16; o2 > 0; o2 >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o2));
+            if (lane == 0 && t0 >= 0 && m) atomicMax(emaxp + t0, m);
+          } else if (target >= 0 && emax_row) {
+            atomicMax(emaxp + target, emax_row);
+          }
         }
       }
     }

@@ -6,9 +6,15 @@
 //   exponents and slice images (the A operands of the half transform).
 // Per nocc: buffers and the two work lists (half transform, exchange).
 // Per build (stream-ordered, no host sync):
-//   C digits (B operand of every panel) -> split GEMM Hfit = Bfit C ->
-//   H digits -> split GEMM Kpart = Hfit Hfit^T (upper tiles, split-K) ->
-//   ordered reduce K = -sum Kpart.
+//   C digits (B operand of every panel) -> split GEMM Hfit = Bfit C (FP64,
+//   row exponents by atomicMax) -> H digits -> split GEMM
+//   Kpart = Hfit Hfit^T (upper tiles, split-K) -> ordered reduce
+//   K = -sum Kpart.
+// With hfuse the half-transform epilogue cuts the digits of Hfit itself
+// (one exponent per AO function and group of 32 auxiliary indices) and the
+// exchange is the segmented variant that applies those exponents.
+// The A operand rows (m, y) of panel I sit at m * pad32(batch) + y, so that
+// every 32-row block is one AO function and one auxiliary group.
 // With the fit folded into the tensor, DF-MO and DF-LMO compute the same
 // K = -(L^-1 B C)^T (L^-1 B C).
 #pragma once
@@ -38,6 +44,13 @@ struct SplitState {
   // auxiliary batching: xb auxiliary rows per batch (nbatch > 1 streams the
   // half transform and the exchange batch by batch; A digits per batch)
   int xb_req = 0, xb = 0, nbatch = 1;
+  // A-row pitch of the full batch: pad32(xb) (pad32(naux) unbatched)
+  int apitch = 0;
+  // fused digit cut of H in the half transform (requested; in effect for
+  // the per-nocc buffers).  Off by default: on GB300 the fused half
+  // transform and segmented exchange together take longer than the FP64 H
+  // round trip and digit pass they replace.
+  bool hfuse = false, hfuse_eff = false;
   SplitJob* d_bjobs = nullptr;  // A-digit jobs, nbatch * nbf (one per (batch, mu))
   int bjob_maxthr = 0;
   std::vector<long long> a_off, eA_off;
@@ -52,6 +65,8 @@ struct SplitState {
   uint16_t* d_Hslices = nullptr;
   int h_nrb = 0, h_nkt = 0, hld = 0;
   int* d_eH = nullptr;
+  int* d_eHs = nullptr;  // fused: exponents [mu][auxiliary group], es_ld per row
+  int es_ld = 0;
   double* d_Kpart = nullptr;
   double* d_dpart = nullptr;  // J partials [mu][Y] from the density columns
   double* d_dt = nullptr;     // L^-1 g
@@ -65,7 +80,6 @@ struct SplitState {
   int* d_err = nullptr;
   const double* d_Cg = nullptr;
   int nsm = 148;
-  bool attr_set = false;
   bool profile = false;
   // set by the caller for one build: event recorded right after the half
   // transform (the fork point of the J column sums), and the number of SMs
@@ -118,6 +132,7 @@ struct SplitState {
     free_(&d_H);
     free_(&d_Hslices);
     free_(&d_eH);
+    free_(&d_eHs);
     free_(&d_Kpart);
     free_(&d_dpart);
     free_(&d_dt);
@@ -197,11 +212,15 @@ struct SplitState {
   // auxiliary rows spans pad32(xbc) * hld columns of H
   static int pad32(int x) { return (x + 31) & ~31; }
 
-  gbjk_status launch_gemm(cudaStream_t st, SplitItem* items, int n, int64_t* launches,
-                          std::string* err, int leave_sms = 0) {
+  // variant: 0 plain, 1 half transform with digit output, 2 segmented exchange
+  bool attr_v[3] = {false, false, false};
+  template <bool kH, bool kS>
+  gbjk_status launch_gemm_v(cudaStream_t st, SplitItem* items, int n, int64_t* launches,
+                            std::string* err, int leave_sms) {
     if (n == 0) return GBJK_OK;
-    if (!attr_set) {
-      if (cudaFuncSetAttribute(k_split_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    const int v = kH ? 1 : (kS ? 2 : 0);
+    if (!attr_v[v]) {
+      if (cudaFuncSetAttribute(k_split_gemm<kH, kS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                kSmemBytes) != cudaSuccess) {
         *err = "cannot reserve shared memory for the split GEMM";
         return GBJK_CUDA_ERROR;
@@ -209,10 +228,10 @@ struct SplitState {
       int dev = 0;
       cudaGetDevice(&dev);
       cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-      attr_set = true;
+      attr_v[v] = true;
     }
     const int grid = std::min(n, std::max(1, nsm - leave_sms));
-    k_split_gemm<<<grid, kThreads, kSmemBytes, st>>>(items, n, d_err, stop_item, spin_ns);
+    k_split_gemm<kH, kS><<<grid, kThreads, kSmemBytes, st>>>(items, n, d_err, stop_item, spin_ns);
     (*launches)++;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -220,6 +239,10 @@ struct SplitState {
       return GBJK_CUDA_ERROR;
     }
     return GBJK_OK;
+  }
+  gbjk_status launch_gemm(cudaStream_t st, SplitItem* items, int n, int64_t* launches,
+                          std::string* err, int leave_sms = 0) {
+    return launch_gemm_v<false, false>(st, items, n, launches, err, leave_sms);
   }
 
   // --- once per tensor: prefit and A-operand digits -----------------------
@@ -235,6 +258,7 @@ struct SplitState {
     xb = (xb_req > 0 && xb_req < naux) ? std::max(32, xb_req & ~31) : naux;
     if (xb > naux) xb = naux;
     nbatch = (naux + xb - 1) / xb;
+    apitch = pad32(xb);
     double* d_Bfit = nullptr;
     if (fitted) {
       d_Bfit = const_cast<double*>(d_B);
@@ -295,14 +319,14 @@ struct SplitState {
     }
     Bfit = d_Bfit;  // the mixed-mode J contracts it in FP64
     // A operands: rows (m, y) of panel I, y < xb (all auxiliary rows when
-    // not batched), columns k
+    // not batched), at m * pad32(batch) + y; columns k
     a_off.assign(nblk, 0);
     eA_off.assign(nblk, 0);
     a_nrb.assign(nblk, 0);
     nkt.assign(nblk, 0);
     long long atot = 0, etot = 0;
     for (int I = 0; I < nblk; ++I) {
-      const long long rows = (long long)bsize[I] * xb;
+      const long long rows = (long long)bsize[I] * apitch;
       a_nrb[I] = cdiv_(rows, kTileM) * (kTileM / 32);
       nkt[I] = std::max(1, cdiv_(panelK[I], kTileK));
       a_off[I] = atot;
@@ -317,25 +341,25 @@ struct SplitState {
       return GBJK_OOM;
     }
     if (nbatch == 1) {
-      std::vector<SplitJob> jobs(nblk);
-      int maxrows = 0;
+      // one job per AO function: its naux rows (m, y) at m * apitch + y
+      std::vector<SplitJob> jobs(nbf);
       long long maxthr = 0;
-      for (int I = 0; I < nblk; ++I) {
-        SplitJob& j = jobs[I];
-        j.src = d_Bfit + panel_off[I];
-        j.rs = panelK[I];
-        j.cs = 1;
-        j.row0 = 0;
-        j.nrows = bsize[I] * naux;
-        j.ncols = panelK[I];
-        j.e = d_eA + eA_off[I];
-        j.e_biased = 0;
-        j.nrb = a_nrb[I];
-        j.nkt = nkt[I];
-        j.dst = d_Aslices + a_off[I];
-        maxrows = std::max(maxrows, j.nrows);
-        maxthr = std::max(maxthr, (long long)(j.nrows / 8 + 2) * j.nkt * 32);
-      }
+      for (int I = 0; I < nblk; ++I)
+        for (int m = 0; m < bsize[I]; ++m) {
+          SplitJob& j = jobs[boff[I] + m];
+          j.src = d_Bfit + panel_off[I] + (long long)m * naux * panelK[I];
+          j.rs = panelK[I];
+          j.cs = 1;
+          j.row0 = m * apitch;
+          j.nrows = naux;
+          j.ncols = panelK[I];
+          j.e = d_eA + eA_off[I];
+          j.e_biased = 0;
+          j.nrb = a_nrb[I];
+          j.nkt = nkt[I];
+          j.dst = d_Aslices + a_off[I];
+          maxthr = std::max(maxthr, (long long)(naux / 8 + 2) * j.nkt * 32);
+        }
       SplitJob* dj = nullptr;
       if (alloc(&dj, jobs.size()) != cudaSuccess) {
         *err = "split path: out of memory";
@@ -344,8 +368,8 @@ struct SplitState {
       cudaMemcpy(dj, jobs.data(), jobs.size() * sizeof(SplitJob), cudaMemcpyHostToDevice);
       {
         Scope sc(this, 2, st);
-        k_row_maxexp<<<dim3(cdiv_((long long)maxrows * 32, 256), nblk), 256, 0, st>>>(dj);
-        k_split_tiles<<<dim3(cdiv_(maxthr, 256), nblk), 256, 0, st>>>(dj);
+        k_row_maxexp<<<dim3(cdiv_((long long)naux * 32, 256), nbf), 256, 0, st>>>(dj);
+        k_split_tiles<<<dim3(cdiv_(maxthr, 256), nbf), 256, 0, st>>>(dj);
         *launches += 2;
       }
       cudaStreamSynchronize(st);
@@ -362,7 +386,7 @@ struct SplitState {
             j.src = d_Bfit + panel_off[I] + ((long long)m * naux + Y0) * panelK[I];
             j.rs = panelK[I];
             j.cs = 1;
-            j.row0 = m * xbc;
+            j.row0 = m * pad32(xbc);
             j.nrows = xbc;
             j.ncols = panelK[I];
             j.e = d_eA + eA_off[I];
@@ -434,8 +458,16 @@ struct SplitState {
       ctot += (long long)c_nrb * nkt[I] * kSlices * kImage;
     }
     hld = nocc_ + (nocc_ & 1);  // even row stride: 16-byte aligned pairs
+    hfuse_eff = hfuse;
+    const bool fuse = hfuse_eff;
+    es_ld = apitch / 32;  // auxiliary groups of a full batch
     const long long hk = (long long)pad32(xb) * hld;
-    h_nkt = cdiv_(hk, kTileK);
+    // exchange k-tiles of a batch: fused, one per (auxiliary group, orbital);
+    // unfused, the FP64 H row of pad32(xbc) * hld values in 32-value tiles
+    auto xk_nkt = [&](int xbc) {
+      return fuse ? (pad32(xbc) / 32) * nocc_ : cdiv_((long long)pad32(xbc) * hld, kTileK);
+    };
+    h_nkt = xk_nkt(xb);
     h_nrb = std::max(cdiv_(nbf, kTileM) * (kTileM / 32), cdiv_(nbf, kTileN) * (kTileN / 32));
     int dev = 0;
     cudaGetDevice(&dev);
@@ -453,25 +485,31 @@ struct SplitState {
     const int xlast = naux - (nbatch - 1) * xb;
     if (xlast != xb) sizes.push_back(xlast);
     ksplit = 1;
-    for (int xbc : sizes)
-      ksplit = std::max(ksplit, exchange_ksplit(cdiv_((long long)pad32(xbc) * hld, kTileK), ntile));
+    for (int xbc : sizes) ksplit = std::max(ksplit, exchange_ksplit(xk_nkt(xbc), ntile));
+    const size_t nH = fuse ? 1 : (size_t)nbf * hk;
+    const size_t nEs = fuse ? (size_t)h_nrb * 32 * es_ld : 1;
     if (alloc(&d_Cslices, (size_t)ctot) != cudaSuccess ||
         alloc(&d_eC, (size_t)nblk * c_nrb * 32) != cudaSuccess ||
-        alloc(&d_H, (size_t)nbf * hk) != cudaSuccess ||
+        alloc(&d_H, nH) != cudaSuccess ||
         alloc(&d_Hslices, (size_t)h_nrb * h_nkt * kSlices * kImage) != cudaSuccess ||
         alloc(&d_eH, (size_t)h_nrb * 32) != cudaSuccess ||
+        alloc(&d_eHs, nEs) != cudaSuccess ||
         alloc(&d_Kpart, (size_t)ksplit * nbf * nbf) != cudaSuccess ||
         alloc(&d_dpart, jfused ? (size_t)nbf * naux : 1) != cudaSuccess ||
         alloc(&d_dt, (size_t)naux) != cudaSuccess ||
         cudaMemsetAsync(d_Cslices, 0, (size_t)ctot * 2, st) != cudaSuccess ||
         cudaMemsetAsync(d_eC, 0, (size_t)nblk * c_nrb * 32 * 4, st) != cudaSuccess ||
-        cudaMemsetAsync(d_H, 0, (size_t)nbf * hk * 8, st) != cudaSuccess ||
+        cudaMemsetAsync(d_H, 0, nH * 8, st) != cudaSuccess ||
         cudaMemsetAsync(d_Hslices, 0, (size_t)h_nrb * h_nkt * kSlices * kImage * 2, st) !=
             cudaSuccess) {
       release_build();
       *err = "split path: out of memory for the per-build buffers";
       return GBJK_OOM;
     }
+    // group exponents of rows that no half transform writes (beyond nbf,
+    // panels without columns) stay "all zero"
+    k_fill_int<<<(int)std::min<size_t>(cdiv_((long long)nEs, 256), 4 * nsm), 256, 0, st>>>(
+        d_eHs, (long long)nEs, -2000);
     std::vector<SplitItem> items;
     std::vector<SplitJob> jobs(2 * nblk);
     plans.clear();
@@ -479,10 +517,11 @@ struct SplitState {
       const int xbc = sizes[pi];
       BatchPlan pl;
       pl.xbc = xbc;
-      // half transform: Hfit rows (m, y) of panel I, columns i (+ density)
+      // half transform: Hfit rows (m, y) of panel I, columns i (+ density);
+      // A rows at m * pad32(xbc) + y
       pl.ht0 = (int)items.size();
       for (int I = 0; I < nblk; ++I) {
-        const long long rows = (long long)bsize[I] * xbc;
+        const long long rows = (long long)bsize[I] * pad32(xbc);
         const int ncolI = nocc_ + (jfused ? bsize[I] : 0);
         for (int mt = 0; mt < cdiv_(rows, kTileM); ++mt)
           for (int nt = 0; nt < cdiv_(ncolI, kTileN); ++nt) {
@@ -497,12 +536,27 @@ struct SplitState {
             w.nkt = nkt[I];
             w.ea = d_eA + eA_off[I] + (long long)mt * kTileM;
             w.eb = d_eC + (long long)I * c_nrb * 32 + (long long)nt * kTileN;
-            // column-pair-outermost layout: each epilogue store is one
-            // contiguous 512-byte run (SplitItem::perm_rs)
-            w.out = d_H + (long long)boff[I] * pad32(xbc) * hld + (long long)nt * kTileN * 32;
-            w.ldr = hld;
-            w.perm_rs = (long long)pad32(xbc) * hld;
-            w.perm_div = xbc;
+            w.apitch = pad32(xbc);
+            w.arow0 = mt * kTileM;
+            w.ay_valid = xbc;
+            if (fuse) {
+              // digits of H rows boff[I] + m, k-tile (y / 32) * nocc + i
+              w.out = nullptr;
+              w.ldr = 0;
+              w.hdig = d_Hslices;
+              w.h_nrb = h_nrb;
+              w.hrow0 = boff[I];
+              w.eseg = d_eHs;
+              w.es_ld = es_ld;
+              w.seg_nkt = nocc_;
+            } else {
+              // column-pair-outermost layout: each epilogue store is one
+              // contiguous 512-byte run (SplitItem::perm_rs)
+              w.out = d_H + (long long)boff[I] * pad32(xbc) * hld + (long long)nt * kTileN * 32;
+              w.ldr = hld;
+              w.perm_rs = (long long)pad32(xbc) * hld;
+              w.perm_div = xbc;
+            }
             w.m_valid = (int)std::min<long long>(kTileM, rows - (long long)mt * kTileM);
             w.n_valid = std::min(kTileN, ncolI - nt * kTileN);
             // row (m, y) of panel I belongs to H row mu = boff[I] + m
@@ -518,7 +572,7 @@ struct SplitState {
       }
       pl.nht = (int)items.size() - pl.ht0;
       // exchange: upper tiles, split over k
-      const int nk_b = cdiv_((long long)pad32(xbc) * hld, kTileK);
+      const int nk_b = xk_nkt(xbc);
       const int ksb = exchange_ksplit(nk_b, ntile);
       const int kt_per = cdiv_(nk_b, ksb);
       pl.ksplit = cdiv_(nk_b, kt_per);
@@ -549,6 +603,14 @@ struct SplitState {
             w.out2 = nullptr;
             w.c0 = 0;
             w.ncol1 = 1 << 30;
+            if (fuse) {
+              // segment g = auxiliary group: nocc k-tiles with the
+              // exponents of (row, g)
+              w.seg_nkt = nocc_;
+              w.esa = d_eHs + (long long)r0 * es_ld;
+              w.esb = d_eHs + (long long)c0 * es_ld;
+              w.es_ld = es_ld;
+            }
             items.push_back(w);
           }
       }
@@ -664,7 +726,7 @@ struct SplitState {
         k_split_tiles<<<dim3(cdiv_((long long)bjob_maxthr, 256), nbf), 256, 0, st>>>(bj);
         *launches += 2;
       }
-      if (nbatch > 1 && pad32(pl.xbc) != pl.xbc) {
+      if (nbatch > 1 && !hfuse_eff && pad32(pl.xbc) != pl.xbc) {
         // the last batch's H layout reuses slots the full batches wrote:
         // clear its unused auxiliary slots
         Scope sc(this, 2, st);
@@ -681,7 +743,11 @@ struct SplitState {
           *err = "split path: memset failed";
           return GBJK_CUDA_ERROR;
         }
-        if ((s = launch_gemm(st, d_items + pl.ht0, pl.nht, launches, err))) return s;
+        if (hfuse_eff)
+          s = launch_gemm_v<true, false>(st, d_items + pl.ht0, pl.nht, launches, err, 0);
+        else
+          s = launch_gemm(st, d_items + pl.ht0, pl.nht, launches, err);
+        if (s) return s;
       }
       if (ev_ht && nbatch == 1 && cudaEventRecord(ev_ht, st) != cudaSuccess) {
         *err = "split path: event record failed";
@@ -690,14 +756,21 @@ struct SplitState {
       {
         Scope sc(this, 2, st);
         k_exp_unbias<<<cdiv_((long long)h_nrb * 32, 256), 256, 0, st>>>(d_eH, h_nrb * 32);
-        const long long hthr =
-            (long long)(nbf / 8 + 2) * cdiv_((long long)pad32(pl.xbc) * hld, kTileK) * 32;
-        k_split_tiles<<<dim3(cdiv_(hthr, 256), 1), 256, 0, st>>>(d_jobs + pl.hjob);
-        *launches += 2;
+        (*launches)++;
+        if (!hfuse_eff) {
+          const long long hthr =
+              (long long)(nbf / 8 + 2) * cdiv_((long long)pad32(pl.xbc) * hld, kTileK) * 32;
+          k_split_tiles<<<dim3(cdiv_(hthr, 256), 1), 256, 0, st>>>(d_jobs + pl.hjob);
+          (*launches)++;
+        }
       }
       {
         Scope sc(this, 1, st);
-        if ((s = launch_gemm(st, d_items + pl.k0, pl.nk, launches, err, k_grid))) return s;
+        if (hfuse_eff)
+          s = launch_gemm_v<false, true>(st, d_items + pl.k0, pl.nk, launches, err, k_grid);
+        else
+          s = launch_gemm(st, d_items + pl.k0, pl.nk, launches, err, k_grid);
+        if (s) return s;
       }
       k_splitk_reduce_acc<<<cdiv_((long long)nbf * nbf, 256), 256, 0, st>>>(
           d_Kpart, pl.ksplit, nbf, -1.0, 1, b > 0 ? 1 : 0, dK);

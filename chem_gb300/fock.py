@@ -80,6 +80,9 @@ def lib():
         L.gbjk_scf_end.argtypes = [vp]
         L.gbjk_get_overlap.argtypes = [vp]
         L.gbjk_get_overlap.restype = C.c_int
+        L.gbjk_set_split_fuse.argtypes = [vp, C.c_int]
+        L.gbjk_get_split_fuse.argtypes = [vp]
+        L.gbjk_get_split_fuse.restype = C.c_int
         L.gbjk_set_fitted.argtypes = [vp, C.c_int]
         L.gbjk_set_aux_batch.argtypes = [vp, C.c_int]
         L.gbjk_set_occ_batch.argtypes = [vp, C.c_int]
@@ -347,6 +350,15 @@ class JKEngine:
 
     def get_overlap(self):
         return int(lib().gbjk_get_overlap(self.h))
+
+    def set_split_fuse(self, on):
+        """Mixed-path exchange digits: cut in the half-transform epilogue
+        with one exponent per (AO function, 32 auxiliary indices) (True), or
+        from an FP64 H with one exponent per AO function (False, default)."""
+        self._check(lib().gbjk_set_split_fuse(self.h, 1 if on else 0), "gbjk_set_split_fuse")
+
+    def get_split_fuse(self):
+        return bool(lib().gbjk_get_split_fuse(self.h))
 
     def set_jmode(self, jmode):
         """'vinv' (reference route, default) or 'cholesky'."""

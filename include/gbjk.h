@@ -162,6 +162,16 @@ gbjk_status gbjk_test_split_stall(gbjk_ctx* ctx, int item, double wait_ms);
 gbjk_status gbjk_set_overlap(gbjk_ctx* ctx, int sms);
 int gbjk_get_overlap(const gbjk_ctx* ctx);
 
+/* Mixed-precision exchange: 1 cuts the digit slices of the half transform
+ * H = (L^-1 B) C in the half-transform epilogue, with one exponent per AO
+ * function and group of 32 auxiliary indices, and the exchange GEMM applies
+ * those exponents per k segment; 0 (default) writes H in FP64 and cuts its
+ * digits in a separate pass with one exponent per AO function.  Both stay
+ * within the split path's accuracy bound; their results differ in the last
+ * bits.  No counterpart in the reference. */
+gbjk_status gbjk_set_split_fuse(gbjk_ctx* ctx, int on);
+int gbjk_get_split_fuse(const gbjk_ctx* ctx);
+
 /* jmode: GBJK_J_VINV (default, the reference route) or GBJK_J_CHOLESKY.
  * No counterpart in the reference. */
 gbjk_status gbjk_set_jmode(gbjk_ctx* ctx, int jmode);

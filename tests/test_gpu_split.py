@@ -63,6 +63,37 @@ def test_split_k_vs_oracle(sysname, request):
     eng.close()
 
 
+@pytest.mark.parametrize("sysname", ["butane", "decane"])
+def test_split_fuse_modes(sysname, request):
+    """Both digit cuts of the half transform H: from an FP64 H with one
+    exponent per AO function (default), and in the half-transform epilogue
+    with one exponent per (AO function, 32 auxiliary indices) and a
+    segmented exchange.  Each is within the K bar of the oracle; the density
+    partials of J come from the same integers, so J is the same bits."""
+    ds = request.getfixturevalue(sysname)
+    C = _core_orbitals(ds)
+    P = C @ C.T
+    eng = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=1e-10, precision="split")
+    assert not eng.get_split_fuse()
+    J0, K0 = eng.compute_jk(2 * P, C, "dfmo")
+    eng.set_split_fuse(True)
+    assert eng.get_split_fuse()
+    J1, K1 = eng.compute_jk(2 * P, C, "dfmo")
+    eng.set_split_fuse(False)
+    eng.set_split_fuse(True)
+    J2, K2 = eng.compute_jk(2 * P, C, "dfmo")
+    eng.close()
+    O = Oracle(ds.layout, ds.B)
+    kc = k_split_plan(ds.nbf, ds.naux, ds.nocc)[1]
+    Kr = O.dfmo_k(np.tril(ds.Linv), C, 1e-10, kchunk=kc)
+    d1, d0 = np.abs(K1 - Kr).max(), np.abs(K0 - Kr).max()
+    print(f"{sysname}: max|dK| fused {d1:.3e}, unfused {d0:.3e}")
+    assert d1 <= 1e-9 and d0 <= 1e-9
+    assert np.array_equal(J1, J0)
+    assert np.array_equal(K1, K2) and np.array_equal(J1, J2)
+    assert np.abs(K1 - K1.T).max() == 0.0
+
+
 def test_split_scf_energy(water):
     from chem_gb300.scf import run_rhf
     ds = water

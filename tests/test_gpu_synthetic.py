@@ -1,7 +1,7 @@
 """Synthetic pre-fitted DF-K workload at a reduced size (nbf 400, naux 1200,
 nocc 60): device-generated tensor, FP64 path bit-exact against the oracle on
 the downloaded tensor, split path (unbatched and auxiliary-batched with a
-short last batch) within 1e-11 of max|K| of FP64."""
+short last batch, both digit cuts of H) within 1e-11 of max|K| of FP64."""
 import numpy as np
 import pytest
 
@@ -25,19 +25,21 @@ def test_synthetic_fp64_split_batched():
     Kr = Oracle(layout, B).dfmo_k(None, C, 0.0, kchunk=kc)
     assert np.array_equal(K64, Kr)
     scale = np.abs(K64).max()
-    for batch in (0, 256):
-        es = JKEngine(layout, None, None, None, fitted=True, synthetic=syn, precision="split",
-                      aux_batch=batch)
-        _, Ks = es.compute_jk(None, C)
-        # a second build on the same buffers gives the same bits (the short
-        # last batch reuses H slots the full batches wrote)
-        _, Ks2 = es.compute_jk(None, C)
-        es.close()
-        assert np.array_equal(Ks, Ks2)
-        d = np.abs(Ks - K64).max()
-        print(f"aux batch {batch}: max|dK| = {d:.3e} of max|K| = {scale:.3e}")
-        assert d <= 1e-11 * scale
-        assert np.abs(Ks - Ks.T).max() == 0.0
+    for fuse in (True, False):
+        for batch in (0, 256):
+            es = JKEngine(layout, None, None, None, fitted=True, synthetic=syn,
+                          precision="split", aux_batch=batch)
+            es.set_split_fuse(fuse)
+            _, Ks = es.compute_jk(None, C)
+            # a second build on the same buffers gives the same bits (the
+            # short last batch reuses H slots the full batches wrote)
+            _, Ks2 = es.compute_jk(None, C)
+            es.close()
+            assert np.array_equal(Ks, Ks2)
+            d = np.abs(Ks - K64).max()
+            print(f"fuse {fuse} aux batch {batch}: max|dK| = {d:.3e} of max|K| = {scale:.3e}")
+            assert d <= 1e-11 * scale
+            assert np.abs(Ks - Ks.T).max() == 0.0
 
 
 def test_synthetic_fp64_batched_matches_oracle():
