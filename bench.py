@@ -782,7 +782,8 @@ def main():
                 "peak_source": "nominal FP64 1.25 TFLOP/s (MEASURED_PEAKS.json has no FP64 figure)",
                 "algorithmic_flops_per_launch": flops64[name], "ms_per_launch": per_launch_ms}
     elif name in ("j_rowdot", "j_colsum"):
-        byts = nnz * 8.0
+        # the mixed path's column sums read the 6-byte compact copy of L^-1 B
+        byts = nnz * (6.0 if args.precision == "split" and name == "j_colsum" else 8.0)
         ach = byts / (per_launch_ms * 1e-3) / 1e9
         roof = {"kernel": name, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s",
                 "frac": ach / hbm, "traffic": None, "peak_source": src,

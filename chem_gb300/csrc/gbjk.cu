@@ -294,7 +294,9 @@ void resolve_profile(gbjk_ctx* ctx) {
 
 int cdiv(long long a, long long b) { return (int)((a + b - 1) / b); }
 // auxiliary rows per block of the mixed-path J column sums
-constexpr int kColsumChunk = 512;
+// auxiliary rows per chunk of the mixed-path J column sums (one warp of 128
+// columns per block: more, shorter blocks keep the grid several waves deep)
+constexpr int kColsumChunk = 256;
 
 // Tiles of tm rows x tn columns: 64 x 64, 64 x 16 (narrow kernel) or
 // 16 x 16 (one thread per output).
@@ -1080,6 +1082,7 @@ gbjk_status gbjk_create(gbjk_ctx** out, const gbjk_desc* d) {
   }
   ctx->split.init(ctx->nbf, ctx->naux, ctx->nblk, ctx->bsize, ctx->boff, ctx->panelK, ctx->cmoff,
                   ctx->panel_off);
+  ctx->split.set_dev_layout(ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff, ctx->d_panelK);
   *out = ctx;
   return GBJK_OK;
 }
@@ -1768,11 +1771,12 @@ static gbjk_status run_jk_split(gbjk_ctx* ctx, const double* dP, const double* d
     }
     {
       PhaseScope ps(ctx, PH_J_COLSUM);
+      // over the 6-byte compact copy of L^-1 B (one warp of 128 columns per block)
       const int xchunk = kColsumChunk, nchunk = cdiv(naux, xchunk);
-      k_j_colsum_f32x2<<<dim3(cdiv(ctx->maxK, 128), nbf, nchunk), 128, xchunk * sizeof(float2),
-                         js>>>(ctx->split.Bfit, ctx->d_panel_off, ctx->d_blk_of, ctx->d_boff,
-                               ctx->d_panelK, ctx->split.d_dt, nbf, naux, xchunk, ctx->maxK,
-                               ctx->d_jpart);
+      k_j_colsum_f32i16<<<dim3(cdiv(ctx->maxK, 128), nbf, nchunk), 32, xchunk * sizeof(float2),
+                          js>>>(ctx->split.d_Bhi, ctx->split.d_Blo, ctx->split.d_cpo, ctx->d_blk_of,
+                                ctx->d_boff, ctx->d_panelK, ctx->split.d_dt, nbf, naux, xchunk,
+                                ctx->maxK, ctx->d_jpart);
       k_j_colsum_chunks<<<dim3(cdiv(ctx->maxK, 128), nbf), 128, 0, js>>>(
           ctx->d_jpart, nchunk, nbf, ctx->maxK, ctx->d_blk_of, ctx->d_panelK, ctx->d_cmoff,
           ctx->d_colmap, dJ);

@@ -40,6 +40,15 @@ struct SplitState {
   bool fitted = false;
   bool bfit_owned = false;
   double* Bfit = nullptr;
+  // compact copy of Bfit for the mixed-path J (k_encode_f32i16: FP32 hi and
+  // a 16-bit remainder per element, 6 bytes; rows padded to a multiple of 8,
+  // panels at d_cpo[I]), unbatched only
+  float* d_Bhi = nullptr;
+  uint16_t* d_Blo = nullptr;
+  long long* d_cpo = nullptr;
+  // the context's device copies of the panel layout (not owned)
+  const long long* dd_panel_off = nullptr;
+  const int *dd_blk_of = nullptr, *dd_boff = nullptr, *dd_panelK = nullptr;
   uint16_t* d_Aslices = nullptr;
   // auxiliary batching: xb auxiliary rows per batch (nbatch > 1 streams the
   // half transform and the exchange batch by batch; A digits per batch)
@@ -96,6 +105,12 @@ struct SplitState {
   int64_t nl[4] = {0, 0, 0, 0};
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> pending;
 
+  void set_dev_layout(const long long* po, const int* blk_of, const int* bo, const int* pk) {
+    dd_panel_off = po;
+    dd_blk_of = blk_of;
+    dd_boff = bo;
+    dd_panelK = pk;
+  }
   void init(int nbf_, int naux_, int nblk_, const std::vector<int>& bs,
             const std::vector<int>& bo, const std::vector<int>& pk, const std::vector<int>& cmo,
             const std::vector<long long>& po) {
@@ -146,6 +161,9 @@ struct SplitState {
     if (bfit_owned) free_(&Bfit);
     Bfit = nullptr;
     bfit_owned = false;
+    free_(&d_Bhi);
+    free_(&d_Blo);
+    free_(&d_cpo);
     free_(&d_Aslices);
     free_(&d_bjobs);
     free_(&d_eA);
@@ -317,7 +335,27 @@ struct SplitState {
       cudaFree(dg);
       cudaFree(dt);
     }
-    Bfit = d_Bfit;  // the mixed-mode J contracts it in FP64
+    Bfit = d_Bfit;
+    if (nbatch == 1) {
+      // the mixed-mode J reads L^-1 B once per build: a 6-byte copy
+      std::vector<long long> cpo(nblk);
+      long long ncomp = 0;
+      for (int I = 0; I < nblk; ++I) {
+        cpo[I] = ncomp;
+        ncomp += (long long)bsize[I] * naux * ((panelK[I] + 7) & ~7);
+      }
+      if (alloc(&d_Bhi, (size_t)ncomp) != cudaSuccess ||
+          alloc(&d_Blo, (size_t)ncomp) != cudaSuccess || alloc(&d_cpo, (size_t)nblk) != cudaSuccess ||
+          cudaMemcpy(d_cpo, cpo.data(), nblk * sizeof(long long), cudaMemcpyHostToDevice) !=
+              cudaSuccess) {
+        *err = "split path: out of memory for the compact J tensor";
+        return GBJK_OOM;
+      }
+      Scope sc(this, 3, st);
+      k_encode_f32i16<<<dim3(naux, nbf), 128, 0, st>>>(d_Bfit, dd_panel_off, d_cpo, dd_blk_of,
+                                                      dd_boff, dd_panelK, naux, d_Bhi, d_Blo);
+      (*launches)++;
+    }
     // A operands: rows (m, y) of panel I, y < xb (all auxiliary rows when
     // not batched), at m * pad32(batch) + y; columns k
     a_off.assign(nblk, 0);
