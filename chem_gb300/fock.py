@@ -345,7 +345,8 @@ class JKEngine:
 
     def set_overlap(self, sms):
         """SMs the mixed-path exchange leaves to the concurrent J column
-        sums (0: phases in order on one stream)."""
+        sums on a second stream (0, default: none, the J blocks co-reside
+        with the exchange CTAs; -1: phases in order on one stream)."""
         self._check(lib().gbjk_set_overlap(self.h, int(sms)), "gbjk_set_overlap")
 
     def get_overlap(self):

@@ -155,10 +155,12 @@ gbjk_status gbjk_upload_b_eri3c(gbjk_ctx* ctx, const gbjk_shells* ao, const gbjk
 gbjk_status gbjk_test_split_stall(gbjk_ctx* ctx, int item, double wait_ms);
 
 /* Mixed-precision build: after the half transform the J column sums
- * (HBM-bound) run on a second stream of the context beside the exchange
- * GEMM (tensor-bound), which then leaves `sms` SMs to them; 0 runs the
- * phases in order on one stream.  Results are the same bits either way.
- * No counterpart in the reference. */
+ * (HBM-bound) run on a second stream of the context beside the digit pass
+ * and the exchange GEMM (tensor-bound), which leaves `sms` SMs to them;
+ * 0 (default) gives the exchange every SM and the J blocks fill the
+ * registers and shared memory its CTAs leave free; -1 runs the phases in
+ * order on one stream.  Results are the same bits either way.  No
+ * counterpart in the reference. */
 gbjk_status gbjk_set_overlap(gbjk_ctx* ctx, int sms);
 int gbjk_get_overlap(const gbjk_ctx* ctx);
 

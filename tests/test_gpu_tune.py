@@ -68,3 +68,40 @@ def test_autotune_and_cache(precision, butane, tmp_path):
     with pytest.raises(RuntimeError):
         e3.autotune(2 * P, C, kmethod="dflmo", reps=0, cache=cache)
     e3.close()
+
+
+def test_split_overlap_modes_same_bits(decane):
+    """The mixed build's J column sums on a second stream co-resident with
+    the exchange (default, 0), beside an exchange that leaves 8 SMs, and in
+    order on one stream (-1), through direct calls and a captured graph:
+    the same bits every time."""
+    import torch
+    ds = decane
+    C = np.ascontiguousarray(_orbitals(ds))
+    P = C @ C.T
+    eng = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=1e-10, precision="split")
+    assert eng.get_overlap() == 0
+    ref = None
+    for mode in (0, -1, 8, 0):
+        eng.set_overlap(mode)
+        assert eng.get_overlap() == mode
+        J, K = eng.compute_jk(2 * P, C)
+        if ref is None:
+            ref = (J, K)
+        assert np.array_equal(J, ref[0]) and np.array_equal(K, ref[1]), mode
+    dev = torch.device("cuda", 0)
+    dP = torch.from_numpy(2 * P).to(dev)
+    dC = torch.from_numpy(C).to(dev)
+    dJ = torch.empty((ds.nbf, ds.nbf), dtype=torch.float64, device=dev)
+    dK = torch.empty_like(dJ)
+    for mode in (0, -1):
+        eng.set_overlap(mode)
+        eng.capture_graph(dP.data_ptr(), dC.data_ptr(), ds.nocc, dJ.data_ptr(), dK.data_ptr())
+        eng.launch_graph()
+        eng.launch_graph()
+        eng.synchronize()
+        assert np.array_equal(dJ.cpu().numpy(), ref[0]), mode
+        assert np.array_equal(dK.cpu().numpy(), ref[1]), mode
+    with pytest.raises(RuntimeError):
+        eng.set_overlap(-2)
+    eng.close()
