@@ -94,6 +94,24 @@ def test_split_fuse_modes(sysname, request):
     assert np.abs(K1 - K1.T).max() == 0.0
 
 
+@pytest.mark.parametrize("aux_batch", [0, 200])
+def test_split_k_block_filter(aux_batch, decane):
+    """The mixed path's K block filter (after the last split-K reduction,
+    unbatched and auxiliary-batched) is the oracle's block filter applied to
+    the unfiltered mixed K, bit for bit, at a threshold where it acts."""
+    ds = decane
+    C = _core_orbitals(ds)
+    out = {}
+    for eps in (0.0, 1e-6):
+        eng = JKEngine(ds.layout, ds.B, np.tril(ds.Linv), ds.Vinv, eps=eps, precision="split",
+                       aux_batch=aux_batch)
+        _, out[eps] = eng.compute_jk(None, C, "dfmo")
+        eng.close()
+    Kf = Oracle(ds.layout, ds.B).filter(out[0.0], 1e-6)
+    assert (Kf == 0).sum() > (out[0.0] == 0).sum()  # the filter acts here
+    assert np.array_equal(out[1e-6], Kf)
+
+
 def test_split_scf_energy(water):
     from chem_gb300.scf import run_rhf
     ds = water
