@@ -316,8 +316,9 @@ gbjk_status gbjk_tune_cache_store(const char* path, const char* sig, const gbjk_
  * file holds this signature the recorded choice is adopted without
  * timing.  Otherwise candidates are timed one dimension at a time (each
  * with one warm-up build and `reps` timed builds, CUDA events on the
- * context's stream), the fastest is kept, and it is appended to the cache
- * when cache_path is given.  A JSON report of the candidates and times goes
+ * context's stream), starting from the built-in rules; a candidate replaces
+ * the choice so far only when it is at least 0.5 % faster.  The choice is
+ * appended to the cache when cache_path is given.  A JSON report of the candidates and times goes
  * to report (at most report_len bytes, may be NULL). */
 gbjk_status gbjk_autotune(gbjk_ctx* ctx, int kmethod, const double* Ptot, const double* Cocc,
                           int nocc, int reps, const char* cache_path, char* report,

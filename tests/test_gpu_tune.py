@@ -52,7 +52,11 @@ def test_autotune_and_cache(precision, butane, tmp_path):
     rep = eng.autotune(2 * P, C, reps=2, cache=cache)
     assert rep["source"] == "timed" and len(rep["candidates"]) >= 4
     assert all(c["ms"] > 0 for c in rep["candidates"])
-    assert rep["best_ms"] == min(c["ms"] for c in rep["candidates"])
+    # the choice is a measured candidate, replaced only by one at least
+    # 0.5 % faster, so within that margin of the fastest
+    fastest = min(c["ms"] for c in rep["candidates"])
+    assert any(c["ms"] == rep["best_ms"] for c in rep["candidates"])
+    assert fastest <= rep["best_ms"] <= fastest / (1 - 0.005) + 1e-12
     J1, K1 = eng.compute_jk(2 * P, C)
     chosen = rep["chosen"]
     eng.close()
