@@ -75,6 +75,7 @@ def footprint_bytes(layout, nocc, precision="split"):
     b += 8 * (nbf * nbf * 4 + nbf * naux)       # P, J, K, partials
     if precision == "split":
         b += 8 * nnz + 11 * nnz                 # L^-1 B (FP64) + digit slices (padded)
+        b += 6.1 * nnz                          # J's compact copy (6 B, rows padded)
         b += 8 * nbf * naux * (nocc + 1)        # fitted half transform
         b += 11 * nbf * naux * (nocc + 1)       # its digits
         b += 8 * nbf * nbf * 64                 # split-K partials (upper bound)
@@ -229,15 +230,17 @@ class FockServer:
 
     def _true_up(self, r):
         """After an engine's first build (all its buffers allocated), replace
-        the admission estimate by its measured device bytes."""
+        the admission estimate by its measured device bytes, in either
+        direction (an estimate that was too low is charged in full)."""
         r.measured = True
         actual = getattr(r.engine, "device_bytes", None)
         if actual is None:
             return
         actual = int(actual * 1.02) + (16 << 20)
-        if actual < r.nbytes:
+        if actual != r.nbytes:
             with self._cv:
-                self._used -= r.nbytes - actual
+                self._used += actual - r.nbytes
+                self.max_used = max(self.max_used, self._used)
                 r.nbytes = actual
                 self._cv.notify_all()
 

@@ -174,3 +174,23 @@ def test_device_setup_worker_shares_the_queue():
     assert any(e[0] == "evict" for e in srv.log)
     for key, B in created:
         assert isinstance(B, tuple) == (routes[key] == "device"), (key, B)
+
+
+def test_true_up_charges_measured_bytes_both_ways():
+    """After an engine's first build its reservation becomes its measured
+    device bytes (plus 2 % and 16 MiB): an estimate that was too high is
+    released, one that was too low is charged in full."""
+    from chem_gb300.serving import _Resident
+
+    class _Eng:
+        def __init__(self, nbytes):
+            self.device_bytes = nbytes
+
+    srv = FockServer(budget_bytes=1 << 40, slots=1, engine_factory=_FakeEngine)
+    for est, actual in ((10 << 30, 4 << 30), (4 << 30, 9 << 30)):
+        r = _Resident(_Eng(actual), est)
+        srv._used = est
+        srv._true_up(r)
+        want = int(actual * 1.02) + (16 << 20)
+        assert r.nbytes == want and srv._used == want and r.measured
+    srv.close()
